@@ -1,0 +1,183 @@
+/*
+ * sable.h — C ABI of the GB300 VBR SpMV/SpMM library (libsable.so).
+ *
+ * The reference (reikdas/SABLE) has no library boundary: its Python code
+ * generator writes one C program per matrix, which reads the matrix and the
+ * dense operand from text files and prints y (src/codegen.py:293-452 SpMV,
+ * :827-937 SpMM).  The entry points below replace that generated executable.
+ * A plan is the GPU counterpart of one generated program: it is built once
+ * from the VBR arrays (the inspector step) and then executed many times.
+ *
+ * Conventions
+ *   - Every function returns SABLE_OK (0) or a negative SABLE_ERR_* code;
+ *     sable_strerror() gives its text, sable_last_error() the detail of the
+ *     most recent failure on the calling thread.
+ *   - Device pointers (`*_dev`) are CUDA global-memory pointers owned by the
+ *     caller.  The plan owns its own device copy of the matrix.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *     All device work is stream-ordered; nothing synchronises the device
+ *     except the *_host entry points, which synchronise `stream`.
+ *   - A plan may be used from one host thread at a time.
+ *   - Values are FP32 on the device.  Index arrays are int32 except block
+ *     value offsets (indx) and CSR row pointers (indptr), which are int64.
+ */
+#ifndef SABLE_H
+#define SABLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SABLE_OK               0
+#define SABLE_ERR_INVALID     -1  /* inconsistent VBR / CSR arrays            */
+#define SABLE_ERR_CUDA        -2  /* a CUDA runtime call failed               */
+#define SABLE_ERR_NOMEM       -3  /* host or device allocation failed         */
+#define SABLE_ERR_UNSUPPORTED -4  /* valid input outside the supported range  */
+#define SABLE_ERR_TIMEOUT     -5  /* a bounded device-side wait ran out       */
+#define SABLE_ERR_ARG         -6  /* null pointer, bad size or bad option     */
+
+typedef struct sable_plan  sable_plan;
+typedef struct sable_batch sable_batch;
+typedef struct sable_mlp   sable_mlp;
+
+/*
+ * A VBR matrix in the reference's compressed (.vbrc) form
+ * (utils/convert_real_to_vbr.py:18-96, read back by utils/fileio.py:66-93):
+ *   rpntr[n_block_rows+1], cpntr[n_block_cols+1]  partition bounds
+ *   bpntrb/bpntre[n_block_rows]   [begin,end) into bindx, -1 = empty row
+ *   bindx[n_blocks]               block column of every stored block,
+ *                                 block-row-major, ascending within a row
+ *   val, indx[n_dense+1]          values of the blocks kept dense, each
+ *                                 column-major h x w, in bindx order
+ *   ublocks[n_ublocks]            ascending ordinals (over bindx) of the
+ *                                 blocks moved to the CSR part
+ *   indptr[n_rows+1], indices, csr_val   global CSR of those blocks
+ * An uncompressed .vbr matrix is the case n_ublocks = 0, n_dense = n_blocks,
+ * indptr = NULL.
+ */
+typedef struct sable_vbrc_desc {
+    int32_t n_rows, n_cols, n_block_rows, n_block_cols;
+    const int32_t *rpntr, *cpntr, *bpntrb, *bpntre, *bindx;
+    int64_t n_blocks;
+    const float   *val;
+    const int64_t *indx;
+    int64_t n_dense;
+    const int32_t *ublocks;
+    int64_t n_ublocks;
+    const int64_t *indptr;
+    const int32_t *indices;
+    const float   *csr_val;
+} sable_vbrc_desc;
+
+/* Plan layout options; zero-initialise for defaults. */
+typedef struct sable_plan_opts {
+    int32_t row_tile;     /* rows per tile, 1..128 (0: 128)                    */
+    int32_t chunk_bytes;  /* target matrix bytes per work item (0: 32768)      */
+    int32_t spmm_tc;      /* 1: dense blocks of SpMM with N >= 32 run as
+                             split-BF16 on the tensor cores                     */
+    int32_t device;       /* CUDA device ordinal (-1: current)                 */
+} sable_plan_opts;
+
+/* Sizes of a built plan (for byte accounting and tests). */
+typedef struct sable_plan_stats {
+    int64_t n_tiles, n_chunks;
+    int64_t dense_values;     /* stored dense values (padding excluded)       */
+    int64_t dense_padded;     /* float slots in the dense panels              */
+    int64_t sparse_nnz;       /* entries in the CSR segments                  */
+    int64_t device_bytes;     /* device memory held by the plan               */
+    int64_t scratch_floats;   /* partial-sum scratch used by split tiles      */
+} sable_plan_stats;
+
+/* Inspector: replaces vbr_spmv_codegen / gen_single_threaded_spmv
+ * (src/codegen.py:1438-1447, 293-452) — validates the arrays, lays the
+ * matrix out for the GPU and uploads it. */
+int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, sable_plan **out);
+int sable_plan_destroy(sable_plan *plan);
+int sable_plan_get_stats(const sable_plan *plan, sable_plan_stats *out);
+/* Host-only inspector run: validates the arrays, builds and bounds-checks
+ * the device layout, and reports its sizes without touching the GPU. */
+int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts, sable_plan_stats *out);
+
+/* Executor, SpMV: y = A x (replaces the timed loop of the generated program,
+ * src/codegen.py:414-439).  x has n_cols floats, y n_rows floats. */
+int sable_spmv(sable_plan *plan, const float *x_dev, float *y_dev, void *stream);
+
+/* Same, from host buffers: copies x in, runs, copies y out, synchronises. */
+int sable_spmv_host(sable_plan *plan, const float *x_host, float *y_host, void *stream);
+
+/* Executor, SpMM: Y = A X with X row-major n_cols x N (leading dimension
+ * ldx), Y row-major n_rows x N (ldy).  Replaces gen_single_threaded_spmm
+ * (src/codegen.py:827-937), whose width is the literal 512.
+ * Requires N % 4 == 0, ldx % 4 == 0, ldy % 4 == 0, 16-byte aligned X and Y. */
+int sable_spmm(sable_plan *plan, const float *X_dev, int64_t ldx, float *Y_dev, int64_t ldy,
+               int32_t N, void *stream);
+int sable_spmm_host(sable_plan *plan, const float *X_host, float *Y_host, int32_t N, void *stream);
+
+/* Per-work-item device durations (ns) of one SpMV / SpMM launch, written to
+ * ns_dev[n_chunks]; used to time blocks for the learned block model (the
+ * GPU counterpart of studies/threshold.py:32-86). */
+int sable_spmv_timed(sable_plan *plan, const float *x_dev, float *y_dev, int64_t *ns_dev, void *stream);
+int sable_spmm_timed(sable_plan *plan, const float *X_dev, float *Y_dev, int32_t N,
+                     int64_t *ns_dev, void *stream);
+/* Tile index of every work item (host array of n_chunks int64). */
+int sable_plan_chunk_tiles(const sable_plan *plan, int64_t *tile_of_chunk);
+
+/*
+ * Batch: many plans (matrices) executed by one persistent kernel over a
+ * shared work queue sorted by class and size.  No reference counterpart (the
+ * reference times matrices one process at a time); widths[i] = 1 runs SpMV on
+ * plan i, widths[i] = N > 1 runs SpMM of width N.
+ */
+typedef struct sable_batch_opts {
+    int32_t ctas_per_sm;  /* persistent CTAs per SM (0: from occupancy)       */
+    int32_t use_graph;    /* 1: capture the launch in a CUDA graph            */
+} sable_batch_opts;
+
+int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t *widths,
+                       const sable_batch_opts *opts, sable_batch **out);
+/* x_devs[i] / y_devs[i]: operand and result of plan i (X/Y row-major, ld = N). */
+int sable_batch_run(sable_batch *batch, const float *const *x_devs, float *const *y_devs, void *stream);
+int sable_batch_destroy(sable_batch *batch);
+
+/* Block features for the block model, one row of 6 floats per stored block
+ * (bindx order): rows, cols, nnz, density, variance of nnz per row, N.
+ * Host-side; `desc` must be uncompressed (all blocks in val). */
+int sable_block_features(const sable_vbrc_desc *desc, int32_t N, float *feat_out);
+
+/*
+ * Block cost model: MLP 6 -> 64 -> 64 -> 2 (ReLU), FP32, predicting the log
+ * device time of the dense and of the sparse form of a block.  It replaces
+ * the pickled RandomForest threshold (models/density_threshold_spmv.pkl,
+ * used at utils/convert_real_to_vbr.py:20,58).  Training and inference run
+ * on the device in this library's own kernels.
+ * Parameter order in flat buffers: W1[64x6], b1[64], W2[64x64], b2[64],
+ * W3[2x64], b3[2] (row-major, out x in) = 4674 floats.
+ */
+#define SABLE_MLP_NPARAMS 4674
+int sable_mlp_create(sable_mlp **out);
+int sable_mlp_destroy(sable_mlp *m);
+int sable_mlp_set_params(sable_mlp *m, const float *params_host);
+int sable_mlp_get_params(const sable_mlp *m, float *params_host);
+/* Feature normalisation: z = (f - mean) / std applied in-kernel. */
+int sable_mlp_set_norm(sable_mlp *m, const float *mean6, const float *std6);
+/* out_dev[n x 2] = MLP(feat_dev[n x 6]). */
+int sable_mlp_infer(sable_mlp *m, const float *feat_dev, int32_t n, float *out_dev, void *stream);
+/* Mean squared error loss and gradient of all parameters over a batch
+ * (grad_dev[SABLE_MLP_NPARAMS], loss_dev[1]); no parameter update. */
+int sable_mlp_loss_grad(sable_mlp *m, const float *feat_dev, const float *target_dev, int32_t n,
+                        float *grad_dev, float *loss_dev, void *stream);
+/* One Adam step on a batch (loss_dev may be NULL). */
+int sable_mlp_train_step(sable_mlp *m, const float *feat_dev, const float *target_dev, int32_t n,
+                         float lr, float *loss_dev, void *stream);
+
+const char *sable_strerror(int code);
+const char *sable_last_error(void);
+/* Library version string. */
+const char *sable_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SABLE_H */

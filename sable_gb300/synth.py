@@ -1,0 +1,267 @@
+"""Seeded synthetic VBR workloads.
+
+The reference's generator (synthesize_matrices/vbr_matrices_gen.py:36-113)
+draws partitions with random_splits (:24-34), picks dense and "sparse"
+blocks at random and fills every stored entry with 1.0.  The workloads here
+follow the same structure with FP32 values and x drawn from U(-1, 1):
+
+  spmv_1000      1000 x 1000, 10 x 10 random partitions, block p = 0.2,
+                 half of the stored blocks fully dense, the rest 10 % dense.
+  spmv_100k      100000 x 100000, 2000 x 2000 partitions of size U[10,100]
+                 (adjusted to sum to 100000), block p = 0.005, density 1.0
+                 w.p. 0.4 else U[0.05, 0.5], uniform or row-clustered.
+  spmm_50k       50000 x 50000, 1000 x 1000 partitions in [20,80], block
+                 p = 0.01, 60 % dense blocks, rest density U[0.05, 0.3].
+  batch_256      256 square matrices, n log-uniform in [1000, 20000],
+                 partitions U[4,128], block p = 0.02, dense fraction
+                 U[0.2, 0.8], sparse density U[0.02, 0.4]; width 64 for half.
+  blocks_200k    standalone blocks for the block model: h, w log-uniform in
+                 [2, 256], density U[0.01, 1], uniform / banded /
+                 row-clustered, N in {1, 8, 32, 128}.
+Every generator is deterministic in its seed (numpy default_rng).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+SEED_BASE = 1000
+
+
+@dataclass
+class VbrMatrix:
+    val: np.ndarray      # float32, all stored blocks, column-major each
+    indx: np.ndarray     # int64
+    bindx: np.ndarray    # int64
+    rpntr: np.ndarray
+    cpntr: np.ndarray
+    bpntrb: np.ndarray
+    bpntre: np.ndarray
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n_rows(self) -> int:
+        return int(self.rpntr[-1])
+
+    @property
+    def n_cols(self) -> int:
+        return int(self.cpntr[-1])
+
+    @property
+    def n_blocks(self) -> int:
+        return len(self.bindx)
+
+    def arrays(self):
+        return self.val, self.indx, self.bindx, self.rpntr, self.cpntr, self.bpntrb, self.bpntre
+
+
+def random_splits(rng, n: int, parts: int) -> np.ndarray:
+    """n split into `parts` positive sizes at distinct uniform cut points
+    (the rule of random_splits, vbr_matrices_gen.py:24-34)."""
+    cuts = np.sort(rng.choice(np.arange(1, n), size=parts - 1, replace=False))
+    return np.diff(np.concatenate([[0], cuts, [n]])).astype(np.int64)
+
+
+def sizes_with_sum(rng, parts: int, lo: int, hi: int, total: int) -> np.ndarray:
+    """`parts` sizes drawn U[lo, hi], then random unit steps (decrements of
+    sizes > lo, or increments of sizes < hi) until they sum to `total`."""
+    s = rng.integers(lo, hi + 1, size=parts).astype(np.int64)
+    diff = int(s.sum()) - total
+    while diff != 0:
+        if diff > 0:
+            elig = np.nonzero(s > lo)[0]
+            k = min(diff, len(elig))
+            pick = rng.choice(elig, size=k, replace=False)
+            s[pick] -= 1
+            diff -= k
+        else:
+            elig = np.nonzero(s < hi)[0]
+            k = min(-diff, len(elig))
+            pick = rng.choice(elig, size=k, replace=False)
+            s[pick] += 1
+            diff += k
+    return s
+
+
+def sizes_until(rng, lo: int, hi: int, total: int) -> np.ndarray:
+    """Sizes drawn U[lo, hi] until they cover `total`; the last one is cut to
+    fit and merged into its neighbour when that would leave it below lo."""
+    out = []
+    acc = 0
+    while acc < total:
+        v = int(rng.integers(lo, hi + 1))
+        out.append(v)
+        acc += v
+    out[-1] -= acc - total
+    if out[-1] < lo and len(out) > 1:
+        out[-2] += out.pop()
+    return np.asarray(out, dtype=np.int64)
+
+
+def block_pattern(rng, h: int, w: int, density: float, pattern: str) -> np.ndarray:
+    """Boolean h x w nonzero mask (column-major flattening is applied later)."""
+    hw = h * w
+    k = int(round(density * hw))
+    k = min(max(k, 1), hw)
+    if k == hw:
+        return np.ones((h, w), dtype=bool)
+    m = np.zeros(hw, dtype=bool)
+    if pattern == "uniform":
+        m[rng.choice(hw, size=k, replace=False)] = True
+        return m.reshape(h, w)
+    if pattern == "row_clustered":
+        r = min(h, max(1, -(-k // w)))
+        r0 = int(rng.integers(0, h - r + 1))
+        sub = np.zeros(r * w, dtype=bool)
+        sub[rng.choice(r * w, size=k, replace=False)] = True
+        mm = np.zeros((h, w), dtype=bool)
+        mm[r0:r0 + r, :] = sub.reshape(r, w)
+        return mm
+    if pattern == "banded":
+        # a diagonal band of the block wide enough to hold k entries
+        ii, jj = np.meshgrid(np.arange(h), np.arange(w), indexing="ij")
+        dist = np.abs(ii * (w / h) - jj).ravel()
+        order = np.argsort(dist, kind="stable")
+        band = order[: min(hw, int(k * 1.5) + 1)]
+        m[rng.choice(band, size=k, replace=False)] = True
+        return m.reshape(h, w)
+    raise ValueError(pattern)
+
+
+def assemble(rng, rsizes, csizes, present: np.ndarray, block_fill) -> VbrMatrix:
+    """Build the VBR arrays from partition sizes and a block presence mask.
+    block_fill(rng, h, w, a, b) returns the h x w float32 block (zeros allowed)."""
+    rpntr = np.concatenate([[0], np.cumsum(rsizes)]).astype(np.int64)
+    cpntr = np.concatenate([[0], np.cumsum(csizes)]).astype(np.int64)
+    nbr = len(rsizes)
+    rows, cols = np.nonzero(present)
+    counts = np.bincount(rows, minlength=nbr)
+    ends = np.cumsum(counts)
+    bpntrb = np.where(counts > 0, ends - counts, -1).astype(np.int64)
+    bpntre = np.where(counts > 0, ends, -1).astype(np.int64)
+    h = rsizes[rows]
+    w = csizes[cols]
+    size = h * w
+    indx = np.concatenate([[0], np.cumsum(size)]).astype(np.int64)
+    val = np.empty(int(indx[-1]), dtype=np.float32)
+    for k in range(len(rows)):
+        blk = block_fill(rng, int(h[k]), int(w[k]), int(rows[k]), int(cols[k]))
+        val[indx[k]: indx[k + 1]] = np.asarray(blk, dtype=np.float32).ravel(order="F")
+    return VbrMatrix(val, indx, cols.astype(np.int64), rpntr, cpntr, bpntrb, bpntre)
+
+
+def _values(rng, h, w):
+    return rng.uniform(-1.0, 1.0, size=(h, w)).astype(np.float32)
+
+
+def spmv_1000(seed: int = SEED_BASE + 0) -> VbrMatrix:
+    rng = np.random.default_rng(seed)
+    rs = random_splits(rng, 1000, 10)
+    cs = random_splits(rng, 1000, 10)
+    present = rng.random((10, 10)) < 0.2
+    dense = rng.random((10, 10)) < 0.5
+
+    def fill(rng, h, w, a, b):
+        v = _values(rng, h, w)
+        if not dense[a, b]:
+            v = v * block_pattern(rng, h, w, 0.10, "uniform")
+        return v
+
+    m = assemble(rng, rs, cs, present, fill)
+    m.meta = {"workload": "spmv_1000", "seed": seed}
+    return m
+
+
+def spmv_100k(seed: int = SEED_BASE + 1, n: int = 100000, parts: int = 2000, p: float = 0.005) -> VbrMatrix:
+    rng = np.random.default_rng(seed)
+    rs = sizes_with_sum(rng, parts, 10, 100, n)
+    cs = sizes_with_sum(rng, parts, 10, 100, n)
+    present = rng.random((parts, parts)) < p
+
+    def fill(rng, h, w, a, b):
+        v = _values(rng, h, w)
+        if rng.random() < 0.4:
+            return v
+        d = rng.uniform(0.05, 0.5)
+        pat = "uniform" if rng.random() < 0.5 else "row_clustered"
+        return v * block_pattern(rng, h, w, d, pat)
+
+    m = assemble(rng, rs, cs, present, fill)
+    m.meta = {"workload": "spmv_100k", "seed": seed, "n": n, "parts": parts, "p": p}
+    return m
+
+
+def spmm_50k(seed: int = SEED_BASE + 2, n: int = 50000, parts: int = 1000, p: float = 0.01) -> VbrMatrix:
+    rng = np.random.default_rng(seed)
+    rs = sizes_with_sum(rng, parts, 20, 80, n)
+    cs = sizes_with_sum(rng, parts, 20, 80, n)
+    present = rng.random((parts, parts)) < p
+
+    def fill(rng, h, w, a, b):
+        v = _values(rng, h, w)
+        if rng.random() < 0.6:
+            return v
+        return v * block_pattern(rng, h, w, rng.uniform(0.05, 0.3), "uniform")
+
+    m = assemble(rng, rs, cs, present, fill)
+    m.meta = {"workload": "spmm_50k", "seed": seed, "n": n, "parts": parts, "p": p}
+    return m
+
+
+def batch_256(seed: int = SEED_BASE + 3, count: int = 256, n_lo: int = 1000, n_hi: int = 20000):
+    """Returns (matrices, widths): widths[i] = 64 for odd i (half of them), 1 otherwise."""
+    rng = np.random.default_rng(seed)
+    mats, widths = [], []
+    for i in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi)))))
+        rs = sizes_until(rng, 4, 128, n)
+        cs = sizes_until(rng, 4, 128, n)
+        present = rng.random((len(rs), len(cs))) < 0.02
+        dense_frac = rng.uniform(0.2, 0.8)
+
+        def fill(rng, h, w, a, b, dense_frac=dense_frac):
+            v = _values(rng, h, w)
+            if rng.random() < dense_frac:
+                return v
+            return v * block_pattern(rng, h, w, rng.uniform(0.02, 0.4), "uniform")
+
+        m = assemble(rng, rs, cs, present, fill)
+        m.meta = {"workload": "batch_256", "index": i, "seed": seed, "n": n}
+        mats.append(m)
+        widths.append(64 if i % 2 == 1 else 1)
+    return mats, widths
+
+
+@dataclass
+class BlockSample:
+    h: int
+    w: int
+    density: float
+    pattern: str
+    N: int
+    block: np.ndarray  # float32 h x w
+
+
+def blocks_200k(seed: int = SEED_BASE + 4, count: int = 200000, lo: int = 2, hi: int = 256):
+    """Standalone blocks for the block model (structure only; values U(-1,1))."""
+    rng = np.random.default_rng(seed)
+    pats = ("uniform", "banded", "row_clustered")
+    Ns = (1, 8, 32, 128)
+    hs = np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.int64)
+    ws = np.exp(rng.uniform(np.log(lo), np.log(hi), size=count)).astype(np.int64)
+    ds = rng.uniform(0.01, 1.0, size=count)
+    ps = rng.integers(0, 3, size=count)
+    nsel = rng.integers(0, 4, size=count)
+    for k in range(count):
+        h, w = int(hs[k]), int(ws[k])
+        mask = block_pattern(rng, h, w, float(ds[k]), pats[ps[k]])
+        yield BlockSample(h, w, float(ds[k]), pats[ps[k]], Ns[nsel[k]], _values(rng, h, w) * mask)
+
+
+def vector(n: int, seed: int) -> np.ndarray:
+    return np.random.default_rng(seed).uniform(-1.0, 1.0, size=n).astype(np.float32)
+
+
+def dense_operand(n: int, N: int, seed: int) -> np.ndarray:
+    return np.random.default_rng(seed).uniform(-1.0, 1.0, size=(n, N)).astype(np.float32)

@@ -1,0 +1,151 @@
+"""SpMV parity on the GPU (libsable through its C ABI) against the FP64
+oracle and the reference's generated C.  Tolerance: per row
+|y_gpu - y_ref| <= 1e-5 * (|A||x|)_row."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from sable_gb300 import blockmodel, convert, synth
+from sable_gb300.plan import Plan
+
+pytestmark = pytest.mark.gpu
+
+
+def plan_and_ref(m, dense_mask, x, **opts):
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense_mask)
+    plan = Plan(comp, **opts)
+    y_ref, yabs = oracle.spmv_vbrc(comp, x.astype(np.float64))
+    return plan, comp, y_ref, yabs
+
+
+def run(plan, x):
+    import torch
+    xd = torch.as_tensor(x).cuda()
+    y = plan.spmv(xd)
+    torch.cuda.synchronize()
+    return y.cpu().numpy()
+
+
+def random_vbr(seed, rsizes, csizes, p, dense_frac=0.5, empty_rows=()):
+    rng = np.random.default_rng(seed)
+    rsizes, csizes = np.asarray(rsizes), np.asarray(csizes)
+    present = rng.random((len(rsizes), len(csizes))) < p
+    for a in empty_rows:
+        present[a, :] = False
+
+    def fill(rng, h, w, a, b):
+        v = rng.uniform(-1, 1, (h, w)).astype(np.float32)
+        if rng.random() < dense_frac:
+            return v
+        return v * synth.block_pattern(rng, h, w, rng.uniform(0.02, 0.5), "uniform")
+
+    return synth.assemble(rng, rsizes, csizes, present, fill)
+
+
+def test_example_canon(golden, cuda):
+    ex = synth.VbrMatrix(*[np.asarray(a) for a in golden.arrays("example_arrays")])
+    ex.val = ex.val.astype(np.float32)
+    plan, comp, y_ref, yabs = plan_and_ref(ex, np.ones(ex.n_blocks, bool), np.ones(11, np.float32))
+    y = run(plan, np.ones(11, np.float32))
+    np.testing.assert_array_equal(y, golden.arr("example_canon", "spmv"))
+
+
+def test_example2_density80_canon(golden, cuda):
+    ex2 = synth.VbrMatrix(*[np.asarray(a) for a in golden.arrays("example2_arrays")])
+    ex2.val = ex2.val.astype(np.float32)
+    bt = convert.block_table(ex2.rpntr, ex2.cpntr, ex2.bpntrb, ex2.bpntre, ex2.bindx, ex2.indx)
+    dense = convert.block_density_pct(convert.block_nnz(ex2.val, bt), bt) > 80
+    plan, comp, y_ref, yabs = plan_and_ref(ex2, dense, np.ones(11, np.float32))
+    np.testing.assert_array_equal(comp.ublocks, golden.arr("example2_vbrc", "ublocks"))
+    y = run(plan, np.ones(11, np.float32))
+    canon = golden.arr("example_canon", "spmv_sparse")
+    np.testing.assert_array_equal(y[: len(canon)], canon)
+
+
+@pytest.mark.parametrize("case,density", [("spmv1000_d0", 0), ("spmv1000_d50", 50), ("spmv1000_rf", None)])
+def test_spmv1000_vs_reference_c(golden, cuda, case, density):
+    meta = golden.meta(case)
+    m = synth.spmv_1000(meta["seed"])
+    x = synth.vector(m.n_cols, meta["x_seed"])
+    model = blockmodel.RFTableModel() if density is None else None
+    dense = convert.choose_dense(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, density=density,
+                                 model=model)
+    plan, comp, y_ref, yabs = plan_and_ref(m, dense, x)
+    y = run(plan, x)
+    r_c = oracle.report(y, golden.arr(case, "y"), yabs)
+    r_o = oracle.report(y, y_ref, yabs)
+    assert r_c["pass"] and r_o["pass"], (r_c, r_o)
+
+
+@pytest.mark.parametrize("row_tile", [128, 64, 17])
+@pytest.mark.parametrize("chunk_bytes", [0, 1024])
+def test_edge_shapes(cuda, row_tile, chunk_bytes):
+    """Tall block rows (tile splits), width-1 / height-1 partitions, empty
+    block rows, tiny work items (split tiles, last-arriver reduction)."""
+    rs = [1, 300, 5, 1, 64, 129, 7, 2, 40]
+    cs = [1, 3, 200, 1, 9, 33, 128, 2, 4, 77]
+    m = random_vbr(7, rs, cs, 0.6, empty_rows=(2,))
+    x = synth.vector(m.n_cols, 8)
+    rng = np.random.default_rng(9)
+    dense = rng.random(m.n_blocks) < 0.5
+    plan, comp, y_ref, yabs = plan_and_ref(m, dense, x, row_tile=row_tile, chunk_bytes=chunk_bytes)
+    y = run(plan, x)
+    r = oracle.report(y, y_ref, yabs)
+    assert r["pass"], r
+    assert np.all(y[m.rpntr[2]:m.rpntr[3]] == 0)
+
+
+@pytest.mark.parametrize("dense_all", [True, False])
+def test_all_dense_all_sparse(cuda, dense_all):
+    m = random_vbr(11, np.full(20, 37), np.full(25, 29), 0.3)
+    x = synth.vector(m.n_cols, 12)
+    plan, comp, y_ref, yabs = plan_and_ref(m, np.full(m.n_blocks, dense_all), x)
+    y = run(plan, x)
+    assert oracle.report(y, y_ref, yabs)["pass"]
+
+
+def test_one_huge_block_row(cuda):
+    """One block row with many blocks: dozens of work items on one tile."""
+    m = random_vbr(13, [96], np.full(400, 50), 0.9, dense_frac=0.7)
+    x = synth.vector(m.n_cols, 14)
+    rng = np.random.default_rng(15)
+    plan, comp, y_ref, yabs = plan_and_ref(m, rng.random(m.n_blocks) < 0.6, x)
+    assert plan.stats()["n_chunks"] > 20
+    y = run(plan, x)
+    assert oracle.report(y, y_ref, yabs)["pass"]
+
+
+def test_deterministic_and_host_entry(cuda):
+    import torch
+    m = synth.spmv_1000()
+    x = synth.vector(m.n_cols, 21)
+    rng = np.random.default_rng(22)
+    plan, comp, y_ref, yabs = plan_and_ref(m, rng.random(m.n_blocks) < 0.5, x, chunk_bytes=2048)
+    xd = torch.as_tensor(x).cuda()
+    y1 = plan.spmv(xd).cpu().numpy()
+    y2 = plan.spmv(xd).cpu().numpy()
+    np.testing.assert_array_equal(y1, y2)
+    y3 = plan.spmv_host(x)
+    np.testing.assert_array_equal(y1, y3)
+    assert oracle.report(y1, y_ref, yabs)["pass"]
+
+
+def test_spmv_100k_full_size(cuda):
+    """The 100000^2 workload (~20k blocks, ~5e7 stored values) at full size
+    against the FP64 oracle, with the learned-form split (dense where the
+    dense encoding is cheaper) and the all-CSR split of the reference RF."""
+    import torch
+    m = synth.spmv_100k()
+    x = synth.vector(m.n_cols, 31)
+    bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+    nnz = convert.block_nnz(m.val, bt)
+    cheaper_dense = 4 * bt.size <= 8 * nnz + 4 * (bt.h + 1)
+    for dense in (cheaper_dense, np.zeros(m.n_blocks, bool)):
+        plan, comp, y_ref, yabs = plan_and_ref(m, dense, x)
+        y = run(plan, x)
+        r = oracle.report(y, y_ref, yabs)
+        assert r["pass"], r
+        # linearity: A(2x) == 2 A(x) exactly (scaling by 2 is exact in FP32)
+        y2 = plan.spmv(torch.as_tensor(2 * x).cuda()).cpu().numpy()
+        np.testing.assert_array_equal(y2, 2 * y)
+        plan.close()
