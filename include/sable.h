@@ -74,10 +74,14 @@ typedef struct sable_vbrc_desc {
 /* Plan layout options; zero-initialise for defaults. */
 typedef struct sable_plan_opts {
     int32_t row_tile;     /* rows per tile, 1..128 (0: 128)                    */
-    int32_t chunk_bytes;  /* target matrix bytes per work item (0: 32768)      */
+    int32_t chunk_bytes;  /* target matrix bytes per work item, 256..98304
+                             (0: 32768)                                        */
     int32_t spmm_tc;      /* 1: dense blocks of SpMM with N >= 32 run as
                              split-BF16 on the tensor cores                     */
     int32_t device;       /* CUDA device ordinal (-1: current)                 */
+    int32_t schedule;     /* 0: one CTA per work item (TMA-staged record);
+                             1: persistent warp workers over an LPT schedule
+                             of tile parts, each with a private TMA ring       */
 } sable_plan_opts;
 
 /* Sizes of a built plan (for byte accounting and tests). */
@@ -104,6 +108,10 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
  * src/codegen.py:414-439).  x has n_cols floats, y n_rows floats. */
 int sable_spmv(sable_plan *plan, const float *x_dev, float *y_dev, void *stream);
 
+/* Synchronises `stream` and reports SABLE_ERR_TIMEOUT (then clears the flag)
+ * if a bounded device-side wait of an earlier launch of this plan ran out. */
+int sable_plan_check(sable_plan *plan, void *stream);
+
 /* Same, from host buffers: copies x in, runs, copies y out, synchronises. */
 int sable_spmv_host(sable_plan *plan, const float *x_host, float *y_host, void *stream);
 
@@ -115,12 +123,13 @@ int sable_spmm(sable_plan *plan, const float *X_dev, int64_t ldx, float *Y_dev, 
                int32_t N, void *stream);
 int sable_spmm_host(sable_plan *plan, const float *X_host, float *Y_host, int32_t N, void *stream);
 
-/* Per-work-item device durations (ns) of one SpMV / SpMM launch, written to
- * ns_dev[n_chunks]; used to time blocks for the learned block model (the
- * GPU counterpart of studies/threshold.py:32-86). */
-int sable_spmv_timed(sable_plan *plan, const float *x_dev, float *y_dev, int64_t *ns_dev, void *stream);
+/* Per-work-item device time (SM clock cycles) of one SpMV / SpMM launch,
+ * written to cycles_dev[n_chunks] (SpMM: [n_slices][n_chunks]); used to
+ * time blocks for the learned block model (the GPU counterpart of
+ * studies/threshold.py:32-86). */
+int sable_spmv_timed(sable_plan *plan, const float *x_dev, float *y_dev, int64_t *cycles_dev, void *stream);
 int sable_spmm_timed(sable_plan *plan, const float *X_dev, float *Y_dev, int32_t N,
-                     int64_t *ns_dev, void *stream);
+                     int64_t *cycles_dev, void *stream);
 /* Tile index of every work item (host array of n_chunks int64). */
 int sable_plan_chunk_tiles(const sable_plan *plan, int64_t *tile_of_chunk);
 

@@ -41,7 +41,8 @@ class VbrcDesc(ctypes.Structure):
 
 
 class PlanOpts(ctypes.Structure):
-    _fields_ = [("row_tile", c_int32), ("chunk_bytes", c_int32), ("spmm_tc", c_int32), ("device", c_int32)]
+    _fields_ = [("row_tile", c_int32), ("chunk_bytes", c_int32), ("spmm_tc", c_int32), ("device", c_int32),
+                ("schedule", c_int32)]
 
 
 class PlanStats(ctypes.Structure):
@@ -61,6 +62,7 @@ SIGNATURES = {
     "sable_plan_destroy": (c_int, [c_void_p]),
     "sable_plan_get_stats": (c_int, [c_void_p, POINTER(PlanStats)]),
     "sable_plan_dry_run": (c_int, [POINTER(VbrcDesc), POINTER(PlanOpts), POINTER(PlanStats)]),
+    "sable_plan_check": (c_int, [c_void_p, c_void_p]),
     "sable_spmv": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "sable_spmv_host": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "sable_spmm": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_void_p]),

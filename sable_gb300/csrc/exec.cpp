@@ -1,5 +1,5 @@
 // Executor entry points of the C ABI: plan upload / destroy, SpMV and SpMM
-// launches (device and host-buffer forms), timed variants.
+// launches (device and host-buffer forms), timed variants, error check.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cstring>
@@ -11,62 +11,113 @@
 namespace sable {
 
 template <typename T>
-static int upload_vec(T **dptr, const std::vector<T> &h, const char *what, int64_t *bytes_acc) {
+static int upload_vec(T **dptr, const T *h, size_t n, const char *what, int64_t *bytes_acc) {
     *dptr = nullptr;
-    size_t bytes = h.size() * sizeof(T);
+    size_t bytes = n * sizeof(T);
     if (bytes == 0) bytes = 16;
     cudaError_t e = cudaMalloc((void **)dptr, bytes);
     if (e != cudaSuccess) return fail(SABLE_ERR_NOMEM, "cudaMalloc %s (%zu bytes): %s", what, bytes, cudaGetErrorString(e));
     *bytes_acc += (int64_t)bytes;
-    if (!h.empty()) {
-        e = cudaMemcpy(*dptr, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (n) {
+        e = cudaMemcpy(*dptr, h, n * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(e, what);
+    } else {
+        e = cudaMemset(*dptr, 0, bytes);
         if (e != cudaSuccess) return cuda_fail(e, what);
     }
     return SABLE_OK;
 }
 
+
 int plan_upload(sable_plan *p, const Layout &L) {
     p->n_rows = L.n_rows;
     p->n_cols = L.n_cols;
-    p->n_chunks = (int64_t)L.chunks.size();
+    p->n_items = (int64_t)L.items.size();
     p->n_partial = L.n_partial;
     p->n_split_tiles = L.n_split_tiles;
-    p->max_quads = L.max_quads;
-    p->max_runs = L.max_runs;
-    p->chunk_tile = L.chunk_tile;
+    p->max_item_bytes = std::max(L.max_item_bytes, 64);
+    p->max_xg_floats = std::max(L.max_xg_floats, 4);
     int64_t bytes = 0;
     int rc;
-    if ((rc = upload_vec(&p->d_panel, L.panel, "panel", &bytes))) return rc;
-    if ((rc = upload_vec(&p->d_sparse, L.sparse, "sparse", &bytes))) return rc;
-    if ((rc = upload_vec(&p->d_runs, L.runs, "runs", &bytes))) return rc;
-    if ((rc = upload_vec(&p->d_chunks, L.chunks, "chunks", &bytes))) return rc;
+    // item table, largest first (one CTA per item launches and the timed form)
+    std::vector<int> desc_order(L.items.size());
+    for (size_t i = 0; i < desc_order.size(); ++i) desc_order[i] = (int)i;
+    std::stable_sort(desc_order.begin(), desc_order.end(),
+                     [&](int a, int b) { return L.items[a].cost > L.items[b].cost; });
+    std::vector<ItemRef> table;
+    p->item_tile.clear();
+    for (int i : desc_order) {
+        table.push_back(L.items[i]);
+        p->item_tile.push_back(L.item_tile[i]);
+    }
+    p->items_host = table;
+    // persistent schedule: parts of tiles, greedy LPT over SMs x resident warp workers
+    int dev_sms = 0;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, p->device);
+    const int per_sm = std::max(1, spmv_warp_workers_per_sm(p->max_item_bytes, p->max_xg_floats));
+    int64_t total_bytes = 0;
+    for (const ItemRef &r : L.items) total_bytes += r.bytes;
+    const int64_t workers = (int64_t)dev_sms * per_sm;
+    // parts of about a quarter of a worker's mean load keep LPT balanced
+    const int64_t part_bytes = std::max<int64_t>(p->item_bytes, total_bytes / std::max<int64_t>(1, 4 * workers));
+    std::vector<WorkRef> work;
+    std::vector<int> wbegin;
+    int64_t pp_floats = 0;
+    build_warp_schedule(L, (int)workers, part_bytes, work, wbegin, pp_floats, p->n_multi, p->n_parts);
+    p->n_ctas = (int)workers;
+    if ((rc = upload_vec(&p->d_records, L.records.data(), L.records.size(), "records", &bytes))) return rc;
+    if ((rc = upload_vec(&p->d_items, table.data(), table.size(), "item table", &bytes))) return rc;
+    if ((rc = upload_vec(&p->d_work, work.data(), work.size(), "worker lists", &bytes))) return rc;
+    if ((rc = upload_vec(&p->d_cta_begin, wbegin.data(), wbegin.size(), "schedule", &bytes))) return rc;
+    std::vector<float> pp((size_t)std::max<int64_t>(pp_floats, 1), 0.f);
+    if ((rc = upload_vec(&p->d_ppartial, pp.data(), pp.size(), "part partials", &bytes))) return rc;
+    std::vector<int> pc((size_t)std::max<int64_t>(p->n_multi, 1), 0);
+    if ((rc = upload_vec(&p->d_pcounters, pc.data(), pc.size(), "part counters", &bytes))) return rc;
     std::vector<float> part((size_t)std::max<int64_t>(L.n_partial, 1), 0.f);
-    if ((rc = upload_vec(&p->d_partial, part, "partial", &bytes))) return rc;
+    if ((rc = upload_vec(&p->d_partial, part.data(), part.size(), "partial", &bytes))) return rc;
     std::vector<int> cnt((size_t)std::max<int32_t>(L.n_split_tiles, 1), 0);
-    if ((rc = upload_vec(&p->d_counters, cnt, "counters", &bytes))) return rc;
+    if ((rc = upload_vec(&p->d_counters, cnt.data(), cnt.size(), "counters", &bytes))) return rc;
+    std::vector<int> err(4, 0);
+    if ((rc = upload_vec(&p->d_error, err.data(), err.size(), "error flag", &bytes))) return rc;
+    int dev_max = 0;
+    cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+    // Plans whose items are too large for a warp worker's ring run one CTA per item.
+    if (spmv_warp_smem(p->max_item_bytes, p->max_xg_floats) > dev_max) p->schedule = SABLE_SCHEDULE_ITEMS;
+    if (spmv_items_smem(p->max_item_bytes, p->max_xg_floats + 4) > dev_max)
+        return fail(SABLE_ERR_UNSUPPORTED, "work items need %d bytes of shared memory (device: %d)",
+                    spmv_items_smem(p->max_item_bytes, p->max_xg_floats + 4), dev_max);
     p->stats.n_tiles = L.n_tiles;
-    p->stats.n_chunks = p->n_chunks;
+    p->stats.n_chunks = p->n_items;
     p->stats.dense_values = L.dense_values;
-    p->stats.dense_padded = (int64_t)L.panel.size() * 4;
+    p->stats.dense_padded = L.dense_padded;
     p->stats.sparse_nnz = L.sparse_nnz;
     p->stats.device_bytes = bytes;
     p->stats.scratch_floats = L.n_partial;
     return SABLE_OK;
 }
 
-SpmvArgs spmv_args(const sable_plan *p, const float *x, float *y, int64_t *cycles) {
-    SpmvArgs a;
+LaunchArgs spmv_args(const sable_plan *p, const float *x, float *y, int64_t *cycles) {
+    LaunchArgs a;
     memset(&a, 0, sizeof a);
-    a.chunks = p->d_chunks;
-    a.panel = p->d_panel;
-    a.sparse = p->d_sparse;
-    a.runs = p->d_runs;
-    a.x = x;
-    a.y = y;
-    a.partial = p->d_partial;
-    a.counters = p->d_counters;
-    a.ns_out = cycles;
-    a.n_chunks = (int)p->n_chunks;
+    a.records = p->d_records;
+    a.items = p->d_items;
+    a.work = p->d_work;
+    a.cta_begin = p->d_cta_begin;
+    a.mats = nullptr;
+    a.mat0.x = x;
+    a.mat0.y = y;
+    a.mat0.partial = p->d_partial;
+    a.mat0.counters = p->d_counters;
+    a.mat0.ppartial = p->d_ppartial;
+    a.mat0.pcounters = p->d_pcounters;
+    a.mat0.ldx = 1;
+    a.mat0.ldy = 1;
+    a.mat0.N = 1;
+    a.cycles = cycles;
+    a.error = p->d_error;
+    a.n_items = (int)p->n_items;
+    a.stage_bytes = p->max_item_bytes;
+    a.xg_floats = (p->max_xg_floats + 3) & ~3;
     return a;
 }
 
@@ -74,8 +125,13 @@ static int run_spmv(sable_plan *p, const float *x, float *y, int64_t *cycles, vo
     if (!p || !x || !y) return fail(SABLE_ERR_ARG, "null argument");
     int rc = set_device(p->device);
     if (rc) return rc;
-    SpmvArgs a = spmv_args(p, x, y, cycles);
-    int e = launch_spmv(a, spmv_smem_bytes(p->max_quads, p->max_runs), cycles != nullptr, stream);
+    LaunchArgs a = spmv_args(p, x, y, cycles);
+    int e;
+    if (cycles || p->schedule == SABLE_SCHEDULE_ITEMS) {
+        e = launch_spmv_items(a, cycles != nullptr, stream);
+    } else {
+        e = launch_spmv_warps(a, p->n_ctas, stream);
+    }
     if (e) return cuda_fail((cudaError_t)e, "spmv launch");
     return SABLE_OK;
 }
@@ -96,7 +152,7 @@ static int ensure_spmm_scratch(sable_plan *p, int nt, int n_slices) {
         if (e != cudaSuccess) return fail(SABLE_ERR_NOMEM, "SpMM scratch: %s", cudaGetErrorString(e));
         p->spmm_partial_cap = need;
     }
-    const int64_t needc = std::max<int64_t>(1, p->n_chunks * n_slices);
+    const int64_t needc = std::max<int64_t>(1, (int64_t)std::max<int32_t>(p->n_split_tiles, 1) * n_slices);
     if (needc > p->spmm_counters_cap) {
         if (p->d_spmm_counters) cudaFree(p->d_spmm_counters);
         p->d_spmm_counters = nullptr;
@@ -132,25 +188,25 @@ static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_
     const int n_slices = (N + nt - 1) / nt;
     rc = ensure_spmm_scratch(p, nt, n_slices);
     if (rc) return rc;
-    SpmmArgs a;
+    LaunchArgs a;
     memset(&a, 0, sizeof a);
-    a.chunks = p->d_chunks;
-    a.panel = p->d_panel;
-    a.sparse = p->d_sparse;
-    a.runs = p->d_runs;
-    a.X = X;
-    a.Y = Y;
-    a.partial = p->d_spmm_partial;
-    a.counters = p->d_spmm_counters;
-    a.ns_out = cycles;
-    a.ldx = ldx;
-    a.ldy = ldy;
-    a.N = N;
-    a.nt = nt;
-    a.n_slices = n_slices;
-    a.n_chunks = (int)p->n_chunks;
-    a.part_stride = p->n_partial * nt;
-    int e = launch_spmm_fp32(a, spmm_smem_bytes(nt, p->max_quads, p->max_runs, p->row_tile), cycles != nullptr, stream);
+    a.records = p->d_records;
+    a.items = p->d_items;
+    a.mat0.x = X;
+    a.mat0.y = Y;
+    a.mat0.partial = p->d_spmm_partial;
+    a.mat0.counters = p->d_spmm_counters;
+    a.mat0.ldx = ldx;
+    a.mat0.ldy = ldy;
+    a.mat0.N = N;
+    a.mat0.pad = std::max<int32_t>(p->n_split_tiles, 1);  // counters per N-slice
+    a.cycles = cycles;
+    a.error = p->d_error;
+    a.n_items = (int)p->n_items;
+    a.stage_bytes = p->max_item_bytes;
+    const int64_t part_stride = p->n_partial * nt;
+    int e = launch_spmm_fp32(a, N, nt, part_stride, cycles != nullptr, stream);
+    (void)n_slices;
     if (e) return cuda_fail((cudaError_t)e, "spmm launch");
     return SABLE_OK;
 }
@@ -186,12 +242,15 @@ int sable_plan_destroy(sable_plan *p) {
     int prev = -1;
     cudaGetDevice(&prev);
     cudaSetDevice(p->device);
-    cudaFree(p->d_panel);
-    cudaFree(p->d_sparse);
-    cudaFree(p->d_runs);
-    cudaFree(p->d_chunks);
+    cudaFree(p->d_records);
+    cudaFree(p->d_items);
+    cudaFree(p->d_work);
+    cudaFree(p->d_cta_begin);
+    cudaFree(p->d_ppartial);
+    cudaFree(p->d_pcounters);
     cudaFree(p->d_partial);
     cudaFree(p->d_counters);
+    cudaFree(p->d_error);
     cudaFree(p->d_spmm_partial);
     cudaFree(p->d_spmm_counters);
     cudaFree(p->d_x);
@@ -199,6 +258,23 @@ int sable_plan_destroy(sable_plan *p) {
     spmm_tc_free(p);
     if (prev >= 0) cudaSetDevice(prev);
     delete p;
+    return SABLE_OK;
+}
+
+int sable_plan_check(sable_plan *p, void *stream) {
+    if (!p) return fail(SABLE_ERR_ARG, "null plan");
+    int rc = set_device(p->device);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int flag = 0;
+    cudaError_t e = cudaMemcpyAsync(&flag, p->d_error, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "plan check");
+    if (flag) {
+        cudaMemsetAsync(p->d_error, 0, sizeof(int), s);
+        cudaStreamSynchronize(s);
+        return fail(SABLE_ERR_TIMEOUT, "a bounded device wait ran out in an earlier launch of this plan");
+    }
     return SABLE_OK;
 }
 

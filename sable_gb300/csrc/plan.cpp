@@ -84,7 +84,6 @@ int validate_vbrc(const sable_vbrc_desc *d) {
         if (d->cpntr[b + 1] <= d->cpntr[b]) return fail(SABLE_ERR_INVALID, "cpntr not strictly increasing at %d", b);
     if (d->rpntr[nbr] != d->n_rows) return fail(SABLE_ERR_INVALID, "rpntr[-1]=%d != n_rows=%d", d->rpntr[nbr], d->n_rows);
     if (d->cpntr[nbc] != d->n_cols) return fail(SABLE_ERR_INVALID, "cpntr[-1]=%d != n_cols=%d", d->cpntr[nbc], d->n_cols);
-    if (d->n_cols > SABLE_MAX_COLS) return fail(SABLE_ERR_UNSUPPORTED, "n_cols=%d above %d", d->n_cols, SABLE_MAX_COLS);
     // Block rows must cover bindx contiguously and in order: the generator
     // numbers blocks in (block row, ascending column) order
     // (src/codegen.py:421-435) and ublocks / indx refer to that numbering.
@@ -147,201 +146,185 @@ static int collect_dense(const sable_vbrc_desc *d, std::vector<std::vector<Dense
 }
 
 // ---------------------------------------------------------------------------
-// Plan construction.
+// Plan construction: tiles -> items -> records.
 // ---------------------------------------------------------------------------
-int build_layout(const sable_vbrc_desc *d, int row_tile, int chunk_bytes, Layout &L) {
+static inline int64_t pad16(int64_t b) { return (b + 15) & ~(int64_t)15; }
+
+int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, Layout &L) {
     std::vector<std::vector<DenseBlock>> rows;
     int rc = collect_dense(d, rows);
     if (rc) return rc;
     L = Layout();
     L.n_rows = d->n_rows;
     L.n_cols = d->n_cols;
-    const int64_t sp_chunk = std::max<int64_t>(32, chunk_bytes / 8);
-    struct TileWork { int32_t row0, h; int64_t panel_f4, nq, sp0, ns; int32_t run_first; };
-    std::vector<TileWork> tiles;
-    // Tile-local column runs (one per dense block): panel column start, x column, width.
-    struct ColRun { int32_t pc, col, w; };
-    std::vector<ColRun> colruns;
-    std::vector<int32_t> tile_colrun_begin;
+    int64_t part_floats = 0;
+    int32_t split_tiles = 0;
+    int64_t tile_id = 0;
+    std::vector<float4> panel;      // tile panel (host scratch)
+    std::vector<int32_t> xcol;      // tile panel column -> x column
+    std::vector<int64_t> tp;        // tile-relative CSR row starts
+
+    auto emit_item = [&](int32_t row0, int32_t h, int64_t q0, int64_t q1, int64_t s0, int64_t s1, int64_t k0,
+                         int32_t tile, int32_t kidx, int32_t nitem, int64_t part_base) {
+        const int32_t nq = (int32_t)(q1 - q0), ns = (int32_t)(s1 - s0);
+        ItemHeader hd;
+        memset(&hd, 0, sizeof hd);
+        hd.row0 = row0;
+        hd.h = h;
+        hd.nq = nq;
+        hd.ns = ns;
+        int64_t off = sizeof(ItemHeader);
+        hd.xcol_off = (int32_t)off;
+        off += 16 * (int64_t)nq;                      // 4 int32 per quad
+        hd.panel_off = (int32_t)off;
+        off += 16 * (int64_t)nq * h;
+        hd.rp_off = (int32_t)off;
+        off += ns > 0 ? pad16(4 * ((int64_t)h + 1)) : 0;
+        hd.csr_off = (int32_t)off;
+        off += pad16(8 * (int64_t)ns);
+        hd.bytes = (int32_t)off;
+        hd.tile = tile;
+        hd.kidx = kidx;
+        hd.nitem = nitem;
+        hd.part_base = part_base;
+        hd.mat = 0;
+        // lanes per CSR row from the mean length of the item's non-empty rows
+        int32_t nonempty = 0;
+        std::vector<int32_t> rp;
+        if (ns > 0) {
+            rp.resize(h + 1);
+            for (int32_t i = 0; i <= h; ++i) rp[i] = (int32_t)std::min<int64_t>(std::max<int64_t>(tp[i] - s0, 0), s1 - s0);
+            for (int32_t i = 0; i < h; ++i) nonempty += rp[i + 1] > rp[i];
+        }
+        const double avg = nonempty ? (double)ns / nonempty : 0.0;
+        hd.g = avg <= 12 ? 4 : avg <= 24 ? 8 : avg <= 48 ? 16 : 32;
+        const int64_t base = (int64_t)L.records.size();
+        L.records.resize(base + hd.bytes, 0);
+        unsigned char *R = L.records.data() + base;
+        memcpy(R, &hd, sizeof hd);
+        memcpy(R + hd.xcol_off, xcol.data() + 4 * q0, 16 * (size_t)nq);
+        memcpy(R + hd.panel_off, panel.data() + q0 * h, 16 * (size_t)nq * h);
+        if (ns > 0) {
+            memcpy(R + hd.rp_off, rp.data(), 4 * (size_t)(h + 1));
+            uint2 *E = reinterpret_cast<uint2 *>(R + hd.csr_off);
+            for (int64_t k = 0; k < ns; ++k) {
+                float v = d->csr_val[k0 + s0 + k];
+                memcpy(&E[k].x, &v, 4);
+                E[k].y = (uint32_t)d->indices[k0 + s0 + k];
+            }
+        }
+        ItemRef ref;
+        ref.off = base;
+        ref.bytes = hd.bytes;
+        ref.cost = hd.bytes;
+        L.items.push_back(ref);
+        L.item_tile.push_back(tile_id);
+        L.max_item_bytes = std::max<int>(L.max_item_bytes, hd.bytes);
+        L.max_xg_floats = std::max<int>(L.max_xg_floats, 4 * nq + ns);
+    };
 
     for (int32_t a = 0; a < d->n_block_rows; ++a) {
         const int32_t r0 = d->rpntr[a], hb = d->rpntr[a + 1] - r0;
         const int32_t nt = (hb + row_tile - 1) / row_tile;
-        for (int32_t t = 0; t < nt; ++t) {
+        int32_t W = 0;
+        for (const DenseBlock &db : rows[a]) W += d->cpntr[db.b + 1] - d->cpntr[db.b];
+        const int64_t nq = (W + 3) / 4;
+        for (int32_t t = 0; t < nt; ++t, ++tile_id) {
             const int32_t lo = (int32_t)((int64_t)hb * t / nt), hi = (int32_t)((int64_t)hb * (t + 1) / nt);
-            TileWork tw;
-            tw.row0 = r0 + lo;
-            tw.h = hi - lo;
-            tw.panel_f4 = (int64_t)L.panel.size();
-            tw.run_first = (int32_t)colruns.size();
-            int32_t W = 0;
-            for (const DenseBlock &db : rows[a]) {
-                const int32_t w = d->cpntr[db.b + 1] - d->cpntr[db.b];
-                colruns.push_back({W, d->cpntr[db.b], w});
-                W += w;
-            }
-            const int64_t nq = (W + 3) / 4;
-            tw.nq = nq;
-            L.panel.resize(L.panel.size() + (size_t)(nq * tw.h), make_float4(0.f, 0.f, 0.f, 0.f));
-            float *P = reinterpret_cast<float *>(L.panel.data() + tw.panel_f4);
+            const int32_t h = hi - lo, row0 = r0 + lo;
+            // tile panel and its x columns
+            panel.assign((size_t)(nq * h), make_float4(0.f, 0.f, 0.f, 0.f));
+            xcol.assign((size_t)(4 * nq), 0);
+            float *P = reinterpret_cast<float *>(panel.data());
             int32_t pc = 0;
             for (const DenseBlock &db : rows[a]) {
-                const int32_t w = d->cpntr[db.b + 1] - d->cpntr[db.b];
+                const int32_t c0 = d->cpntr[db.b], w = d->cpntr[db.b + 1] - c0;
                 const float *blk = d->val + db.off;
                 for (int32_t j = 0; j < w; ++j, ++pc) {
+                    xcol[pc] = c0 + j;
                     const int64_t q = pc >> 2, comp = pc & 3;
                     const float *colv = blk + (int64_t)j * hb + lo;
-                    float *dst = P + (q * tw.h) * 4 + comp;
-                    for (int32_t i = 0; i < tw.h; ++i) dst[(int64_t)i * 4] = colv[i];
+                    float *dst = P + (q * h) * 4 + comp;
+                    for (int32_t i = 0; i < h; ++i) dst[(int64_t)i * 4] = colv[i];
                 }
-                L.dense_values += (int64_t)w * tw.h;
             }
-            // CSR entries of the tile's rows
-            tw.sp0 = (int64_t)L.sparse.size();
-            tw.ns = 0;
+            L.dense_values += (int64_t)W * h;
+            L.dense_padded += 4 * nq * h;
+            // CSR rows of the tile
+            int64_t k0 = 0, ns = 0;
+            tp.assign((size_t)h + 1, 0);
             if (d->indptr) {
-                for (int32_t i = 0; i < tw.h; ++i) {
-                    const int32_t r = tw.row0 + i;
-                    for (int64_t k = d->indptr[r]; k < d->indptr[r + 1]; ++k) {
-                        uint2 e;
-                        float v = d->csr_val[k];
-                        memcpy(&e.x, &v, 4);
-                        e.y = (uint32_t)d->indices[k] | ((uint32_t)i << SABLE_COL_BITS);
-                        L.sparse.push_back(e);
-                    }
-                }
-                tw.ns = (int64_t)L.sparse.size() - tw.sp0;
+                k0 = d->indptr[row0];
+                ns = d->indptr[row0 + h] - k0;
+                for (int32_t i = 0; i <= h; ++i) tp[i] = d->indptr[row0 + i] - k0;
             }
-            tiles.push_back(tw);
-            tile_colrun_begin.push_back(tw.run_first);
-        }
-    }
-    tile_colrun_begin.push_back((int32_t)colruns.size());
-    L.n_tiles = (int64_t)tiles.size();
-
-    // Work items.
-    int64_t part_floats = 0;
-    int32_t split_tiles = 0;
-    std::vector<std::pair<int64_t, Chunk>> work;  // (bytes, chunk)
-    for (size_t ti = 0; ti < tiles.size(); ++ti) {
-        const TileWork &tw = tiles[ti];
-        const int32_t cr0 = tile_colrun_begin[ti], cr1 = tile_colrun_begin[ti + 1];
-        const int64_t dense_bytes = 16 * tw.nq * tw.h, sp_bytes = 8 * tw.ns;
-        // dense pieces: [q0, q1) quads
-        std::vector<std::pair<int64_t, int64_t>> dpieces;
-        const int64_t qcap = std::max<int64_t>(1, std::min<int64_t>(SABLE_MAX_CHUNK_QUADS, chunk_bytes / (16 * tw.h)));
-        bool single = (dense_bytes + sp_bytes) <= (chunk_bytes + chunk_bytes / 4) && tw.nq <= SABLE_MAX_CHUNK_QUADS &&
-                      tw.ns <= INT32_MAX && (cr1 - cr0) <= SABLE_MAX_CHUNK_RUNS;
-        if (single) {
-            dpieces.push_back({0, tw.nq});
-        } else {
-            int64_t q0 = 0;
-            int32_t r = cr0;
-            while (q0 < tw.nq) {
-                int64_t q1 = std::min(tw.nq, q0 + qcap);
-                // keep the number of column runs of the piece within the table size
-                while (r < cr1 && colruns[r].pc + colruns[r].w <= 4 * q0) ++r;
-                int32_t rr = r, nrun = 0;
-                while (rr < cr1 && colruns[rr].pc < 4 * q1) {
-                    if (++nrun > SABLE_MAX_CHUNK_RUNS) { q1 = std::max<int64_t>(q0 + 1, colruns[rr].pc / 4); break; }
-                    ++rr;
-                }
-                dpieces.push_back({q0, q1});
-                q0 = q1;
+            L.sparse_nnz += ns;
+            // cut into items
+            const int64_t hdr = sizeof(ItemHeader);
+            const int64_t total = hdr + 16 * nq + 16 * nq * h + (ns ? pad16(4 * ((int64_t)h + 1)) + pad16(8 * ns) : 0);
+            if (total <= item_bytes + item_bytes / 4) {
+                emit_item(row0, h, 0, nq, 0, ns, k0, -1, 0, 1, 0);
+                continue;
+            }
+            const int64_t qcap = std::max<int64_t>(1, (item_bytes - hdr) / (16 * ((int64_t)h + 1)));
+            const int64_t scap = std::max<int64_t>(2, (item_bytes - hdr - pad16(4 * ((int64_t)h + 1))) / 8) & ~(int64_t)1;
+            const int32_t nd = (int32_t)((nq + qcap - 1) / qcap), nsp = (int32_t)((ns + scap - 1) / scap);
+            const int32_t nitem = nd + nsp;
+            const int32_t sid = split_tiles++;
+            const int64_t pbase = part_floats;
+            part_floats += (int64_t)nitem * h;
+            int32_t kidx = 0;
+            for (int32_t k = 0; k < nd; ++k) {
+                const int64_t q0 = nq * k / nd, q1 = nq * (k + 1) / nd;
+                emit_item(row0, h, q0, q1, 0, 0, k0, sid, kidx++, nitem, pbase);
+            }
+            for (int32_t k = 0; k < nsp; ++k) {
+                const int64_t s0 = (ns * k / nsp) & ~(int64_t)0, s1 = ns * (k + 1) / nsp;
+                emit_item(row0, h, 0, 0, s0, s1, k0, sid, kidx++, nitem, pbase);
             }
         }
-        std::vector<std::pair<int64_t, int64_t>> spieces;
-        if (single) {
-            if (tw.ns > 0) spieces.push_back({0, tw.ns});
-        } else {
-            for (int64_t s0 = 0; s0 < tw.ns; s0 += sp_chunk) spieces.push_back({s0, std::min(tw.ns, s0 + sp_chunk)});
-        }
-        int32_t nchunk = single ? 1 : (int32_t)(dpieces.size() + spieces.size());
-        if (nchunk == 0) nchunk = 1;  // zero tile (no stored blocks): writes zeros
-        if (single && dpieces.empty()) dpieces.push_back({0, 0});
-        const int32_t split_id = nchunk > 1 ? split_tiles++ : -1;
-        const int64_t pbase = nchunk > 1 ? part_floats : 0;
-        if (nchunk > 1) part_floats += (int64_t)nchunk * tw.h;
-        int32_t kidx = 0;
-        auto emit = [&](int64_t q0, int64_t q1, int64_t s0, int64_t s1) {
-            Chunk c;
-            memset(&c, 0, sizeof c);
-            c.panel_f4 = tw.panel_f4 + q0 * tw.h;
-            c.sp0 = tw.sp0 + s0;
-            c.part_base = pbase;
-            c.row0 = tw.row0;
-            c.h = tw.h;
-            c.nq = (int32_t)(q1 - q0);
-            c.ns = (int32_t)(s1 - s0);
-            c.run0 = (int32_t)L.runs.size();
-            for (int32_t r = cr0; r < cr1 && c.nq > 0; ++r) {
-                const int64_t a0 = std::max<int64_t>(colruns[r].pc, 4 * q0);
-                const int64_t a1 = std::min<int64_t>(colruns[r].pc + colruns[r].w, 4 * q1);
-                if (a0 >= a1) continue;
-                L.runs.push_back(make_int4((int)(a0 - 4 * q0), (int)(colruns[r].col + (a0 - colruns[r].pc)), (int)(a1 - a0), 0));
-            }
-            c.nrun = (int32_t)L.runs.size() - c.run0;
-            c.tile = split_id;
-            c.kidx = kidx++;
-            c.nchunk = nchunk;
-            L.max_quads = std::max<int>(L.max_quads, c.nq);
-            L.max_runs = std::max<int>(L.max_runs, c.nrun);
-            const int64_t bytes = 16 * (int64_t)c.nq * c.h + 8 * (int64_t)c.ns;
-            work.push_back({bytes, c});
-            L.chunk_tile.push_back((int64_t)ti);
-        };
-        if (single) {
-            emit(dpieces[0].first, dpieces[0].second, spieces.empty() ? 0 : spieces[0].first,
-                 spieces.empty() ? 0 : spieces[0].second);
-        } else {
-            for (auto &p : dpieces) emit(p.first, p.second, 0, 0);
-            for (auto &p : spieces) emit(0, 0, p.first, p.second);
-        }
     }
-    // Largest work first (the hardware scheduler then behaves like greedy LPT).
-    std::vector<size_t> order(work.size());
-    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return work[x].first > work[y].first; });
-    L.chunks.resize(work.size());
-    std::vector<int64_t> ct(work.size());
-    for (size_t i = 0; i < order.size(); ++i) {
-        L.chunks[i] = work[order[i]].second;
-        ct[i] = L.chunk_tile[order[i]];
-    }
-    L.chunk_tile.swap(ct);
+    L.n_tiles = tile_id;
     L.n_partial = part_floats;
     L.n_split_tiles = split_tiles;
-    L.sparse_nnz = (int64_t)L.sparse.size();
     return check_layout(L);
 }
 
 // Every index a kernel will follow, checked on the host before upload.
 int check_layout(const Layout &L) {
-    const int64_t npanel = (int64_t)L.panel.size(), nsp = (int64_t)L.sparse.size(), nruns = (int64_t)L.runs.size();
-    for (size_t k = 0; k < L.chunks.size(); ++k) {
-        const Chunk &c = L.chunks[k];
-        if (c.h < 1 || c.h > SABLE_MAX_ROW_TILE || c.row0 < 0 || c.row0 + c.h > L.n_rows)
-            return fail(SABLE_ERR_INVALID, "layout: chunk %zu rows out of range", k);
-        if (c.nq < 0 || c.nq > SABLE_MAX_CHUNK_QUADS || c.panel_f4 < 0 || c.panel_f4 + (int64_t)c.nq * c.h > npanel)
-            return fail(SABLE_ERR_INVALID, "layout: chunk %zu panel range out of bounds", k);
-        if (c.ns < 0 || c.sp0 < 0 || c.sp0 + c.ns > nsp) return fail(SABLE_ERR_INVALID, "layout: chunk %zu sparse range", k);
-        if (c.nrun < 0 || c.nrun > SABLE_MAX_CHUNK_RUNS || c.run0 < 0 || c.run0 + c.nrun > nruns)
-            return fail(SABLE_ERR_INVALID, "layout: chunk %zu run range", k);
-        if (c.nq > 0 && c.nrun == 0) return fail(SABLE_ERR_INVALID, "layout: chunk %zu has quads but no runs", k);
-        for (int r = 0; r < c.nrun; ++r) {
-            const int4 run = L.runs[c.run0 + r];
-            if (run.x < 0 || run.z < 1 || run.x + run.z > 4 * c.nq || run.y < 0 || run.y + run.z > L.n_cols ||
-                (r > 0 && run.x < L.runs[c.run0 + r - 1].x + L.runs[c.run0 + r - 1].z))
-                return fail(SABLE_ERR_INVALID, "layout: chunk %zu run %d out of bounds", k, r);
+    const int64_t nrec = (int64_t)L.records.size();
+    for (size_t k = 0; k < L.items.size(); ++k) {
+        const ItemRef &r = L.items[k];
+        if (r.off < 0 || (r.off & 15) || r.bytes < (int)sizeof(ItemHeader) || (r.bytes & 15) || r.off + r.bytes > nrec ||
+            r.bytes > SABLE_MAX_ITEM_BYTES)
+            return fail(SABLE_ERR_INVALID, "layout: item %zu record range", k);
+        ItemHeader hd;
+        memcpy(&hd, L.records.data() + r.off, sizeof hd);
+        if (hd.bytes != r.bytes) return fail(SABLE_ERR_INVALID, "layout: item %zu size mismatch", k);
+        if (hd.h < 1 || hd.h > SABLE_MAX_ROW_TILE || hd.row0 < 0 || hd.row0 + hd.h > L.n_rows)
+            return fail(SABLE_ERR_INVALID, "layout: item %zu rows out of range", k);
+        if (hd.nq < 0 || hd.ns < 0 || hd.xcol_off != (int)sizeof(ItemHeader) ||
+            hd.panel_off != hd.xcol_off + 16 * hd.nq || (int64_t)hd.rp_off != hd.panel_off + 16 * (int64_t)hd.nq * hd.h ||
+            hd.csr_off < hd.rp_off || (int64_t)hd.csr_off + 8 * (int64_t)hd.ns > hd.bytes)
+            return fail(SABLE_ERR_INVALID, "layout: item %zu part offsets", k);
+        const unsigned char *R = L.records.data() + r.off;
+        const int32_t *xc = reinterpret_cast<const int32_t *>(R + hd.xcol_off);
+        for (int i = 0; i < 4 * hd.nq; ++i)
+            if (xc[i] < 0 || xc[i] >= L.n_cols) return fail(SABLE_ERR_INVALID, "layout: item %zu x column", k);
+        if (hd.ns > 0) {
+            const int32_t *rp = reinterpret_cast<const int32_t *>(R + hd.rp_off);
+            if (rp[0] != 0 || rp[hd.h] != hd.ns) return fail(SABLE_ERR_INVALID, "layout: item %zu row pointers", k);
+            for (int i = 0; i < hd.h; ++i)
+                if (rp[i + 1] < rp[i]) return fail(SABLE_ERR_INVALID, "layout: item %zu row pointers decrease", k);
+            const uint2 *E = reinterpret_cast<const uint2 *>(R + hd.csr_off);
+            for (int i = 0; i < hd.ns; ++i)
+                if ((int64_t)E[i].y >= L.n_cols) return fail(SABLE_ERR_INVALID, "layout: item %zu CSR column", k);
         }
-        for (int64_t e = c.sp0; e < c.sp0 + c.ns; ++e) {
-            const uint32_t col = L.sparse[e].y & SABLE_COL_MASK, lrow = L.sparse[e].y >> SABLE_COL_BITS;
-            if ((int64_t)col >= L.n_cols || (int)lrow >= c.h) return fail(SABLE_ERR_INVALID, "layout: sparse entry %lld", (long long)e);
-        }
-        if (c.nchunk < 1 || c.kidx < 0 || c.kidx >= c.nchunk) return fail(SABLE_ERR_INVALID, "layout: chunk %zu numbering", k);
-        if (c.nchunk > 1 && (c.tile < 0 || c.tile >= L.n_split_tiles || c.part_base < 0 ||
-                             c.part_base + (int64_t)c.nchunk * c.h > L.n_partial))
-            return fail(SABLE_ERR_INVALID, "layout: chunk %zu split-tile scratch out of bounds", k);
+        if (hd.g != 4 && hd.g != 8 && hd.g != 16 && hd.g != 32) return fail(SABLE_ERR_INVALID, "layout: item %zu lane group", k);
+        if (hd.nitem < 1 || hd.kidx < 0 || hd.kidx >= hd.nitem) return fail(SABLE_ERR_INVALID, "layout: item %zu numbering", k);
+        if (hd.nitem > 1 && (hd.tile < 0 || hd.tile >= L.n_split_tiles || hd.part_base < 0 ||
+                             hd.part_base + (int64_t)hd.nitem * hd.h > L.n_partial))
+            return fail(SABLE_ERR_INVALID, "layout: item %zu split-tile scratch out of bounds", k);
     }
     return SABLE_OK;
 }
@@ -377,9 +360,11 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
     o.device = -1;
     if (opts) o = *opts;
     const int row_tile = o.row_tile ? o.row_tile : SABLE_MAX_ROW_TILE;
-    const int chunk_bytes = o.chunk_bytes ? o.chunk_bytes : 32768;
+    const int chunk_bytes = o.chunk_bytes ? o.chunk_bytes
+                                          : (o.schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES : SABLE_WARP_ITEM_BYTES);
     if (row_tile < 1 || row_tile > SABLE_MAX_ROW_TILE) return fail(SABLE_ERR_ARG, "row_tile %d outside 1..128", row_tile);
-    if (chunk_bytes < 256 || chunk_bytes > (64 << 20)) return fail(SABLE_ERR_ARG, "chunk_bytes %d outside 256..64M", chunk_bytes);
+    if (chunk_bytes < 4096 || chunk_bytes > SABLE_MAX_ITEM_BYTES * 4 / 5)
+        return fail(SABLE_ERR_ARG, "chunk_bytes %d outside 4096..%d", chunk_bytes, SABLE_MAX_ITEM_BYTES * 4 / 5);
     int rc = validate_vbrc(desc);
     if (rc) return rc;
     rc = set_device(o.device);
@@ -388,7 +373,12 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
     if (!p) return fail(SABLE_ERR_NOMEM, "host allocation");
     cudaGetDevice(&p->device);
     p->row_tile = row_tile;
-    p->chunk_bytes = chunk_bytes;
+    p->item_bytes = chunk_bytes;
+    if (o.schedule != SABLE_SCHEDULE_ITEMS && o.schedule != SABLE_SCHEDULE_PERSISTENT) {
+        delete p;
+        return fail(SABLE_ERR_ARG, "schedule %d unknown", o.schedule);
+    }
+    p->schedule = o.schedule;
     p->spmm_tc = o.spmm_tc;
     Layout L;
     rc = build_layout(desc, row_tile, chunk_bytes, L);
@@ -402,9 +392,10 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
 int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts, sable_plan_stats *out) {
     if (!out) return fail(SABLE_ERR_ARG, "null output pointer");
     const int row_tile = opts && opts->row_tile ? opts->row_tile : SABLE_MAX_ROW_TILE;
-    const int chunk_bytes = opts && opts->chunk_bytes ? opts->chunk_bytes : 32768;
+    const int chunk_bytes = opts && opts->chunk_bytes ? opts->chunk_bytes
+                            : (opts && opts->schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES : SABLE_WARP_ITEM_BYTES);
     if (row_tile < 1 || row_tile > SABLE_MAX_ROW_TILE) return fail(SABLE_ERR_ARG, "row_tile %d outside 1..128", row_tile);
-    if (chunk_bytes < 256 || chunk_bytes > (64 << 20)) return fail(SABLE_ERR_ARG, "chunk_bytes outside 256..64M");
+    if (chunk_bytes < 4096 || chunk_bytes > SABLE_MAX_ITEM_BYTES * 4 / 5) return fail(SABLE_ERR_ARG, "chunk_bytes outside range");
     int rc = validate_vbrc(desc);
     if (rc) return rc;
     Layout L;
@@ -412,12 +403,12 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
     if (rc) return rc;
     memset(out, 0, sizeof *out);
     out->n_tiles = L.n_tiles;
-    out->n_chunks = (int64_t)L.chunks.size();
+    out->n_chunks = (int64_t)L.items.size();
     out->dense_values = L.dense_values;
-    out->dense_padded = (int64_t)L.panel.size() * 4;
+    out->dense_padded = L.dense_padded;
     out->sparse_nnz = L.sparse_nnz;
-    out->device_bytes = (int64_t)(L.panel.size() * 16 + L.sparse.size() * 8 + L.runs.size() * 16 +
-                                  L.chunks.size() * sizeof(Chunk) + (L.n_partial + L.n_split_tiles) * 4);
+    out->device_bytes = (int64_t)L.records.size() + (int64_t)L.items.size() * (int64_t)sizeof(ItemRef) +
+                        (L.n_partial + L.n_split_tiles) * 4;
     out->scratch_floats = L.n_partial;
     return SABLE_OK;
 }
@@ -430,7 +421,7 @@ int sable_plan_get_stats(const sable_plan *plan, sable_plan_stats *out) {
 
 int sable_plan_chunk_tiles(const sable_plan *plan, int64_t *tile_of_chunk) {
     if (!plan || !tile_of_chunk) return fail(SABLE_ERR_ARG, "null argument");
-    memcpy(tile_of_chunk, plan->chunk_tile.data(), plan->chunk_tile.size() * sizeof(int64_t));
+    memcpy(tile_of_chunk, plan->item_tile.data(), plan->item_tile.size() * sizeof(int64_t));
     return SABLE_OK;
 }
 

@@ -12,40 +12,50 @@ namespace sable {
 // Host image of a plan's device layout (see sable_internal.h).
 struct Layout {
     int32_t n_rows = 0, n_cols = 0;
-    std::vector<float4> panel;
-    std::vector<uint2> sparse;
-    std::vector<int4> runs;
-    std::vector<Chunk> chunks;
-    std::vector<int64_t> chunk_tile;
-    int64_t n_tiles = 0, n_partial = 0, dense_values = 0, sparse_nnz = 0;
+    std::vector<unsigned char> records;   // item records, 16-byte aligned
+    std::vector<ItemRef> items;           // in record order
+    std::vector<int64_t> item_tile;       // tile of each item
+    int64_t n_tiles = 0, n_partial = 0, dense_values = 0, dense_padded = 0, sparse_nnz = 0;
     int32_t n_split_tiles = 0;
-    int max_quads = 0, max_runs = 0;
+    int max_item_bytes = 0;
+    int max_xg_floats = 0;      // largest 4 nq + ns over items
 };
 
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 int set_device(int dev);
 int validate_vbrc(const sable_vbrc_desc *d);
-int build_layout(const sable_vbrc_desc *d, int row_tile, int chunk_bytes, Layout &L);
+int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, Layout &L);
 int check_layout(const Layout &L);
+// Persistent schedule: tiles' items grouped into parts of <= part_bytes,
+// parts assigned to n_workers warp workers by greedy LPT (schedule.cpp).
+int build_warp_schedule(const Layout &L, int n_workers, int64_t part_bytes, std::vector<WorkRef> &work,
+                        std::vector<int> &begin, int64_t &ppartial_floats, int64_t &n_multi, int64_t &n_parts);
 
 }  // namespace sable
 
 struct sable_plan {
     int device = 0;
     int32_t n_rows = 0, n_cols = 0;
-    int row_tile = 0, chunk_bytes = 0, spmm_tc = 0;
-    float4 *d_panel = nullptr;
-    uint2 *d_sparse = nullptr;
-    int4 *d_runs = nullptr;
-    Chunk *d_chunks = nullptr;
+    int row_tile = 0, item_bytes = 0, spmm_tc = 0, schedule = 0;
+    unsigned char *d_records = nullptr;
+    ItemRef *d_items = nullptr;          // item table, largest first
+    WorkRef *d_work = nullptr;           // warp-worker lists (persistent schedule)
+    int *d_cta_begin = nullptr;          // worker ranges into d_work
+    int n_ctas = 0;                      // warp workers of the persistent schedule
+    float *d_ppartial = nullptr;         // multi-part tile partials
+    int *d_pcounters = nullptr;          // multi-part tile counters
+    int64_t n_parts = 0, n_multi = 0;
     float *d_partial = nullptr;
     int *d_counters = nullptr;
-    int64_t n_chunks = 0, n_partial = 0;
+    int *d_error = nullptr;
+    int64_t n_items = 0, n_partial = 0;
     int32_t n_split_tiles = 0;
-    int max_quads = 0, max_runs = 0;
+    int max_item_bytes = 0;
+    int max_xg_floats = 0;
     sable_plan_stats stats{};
-    std::vector<int64_t> chunk_tile;
+    std::vector<int64_t> item_tile;      // tile of each item (item table order)
+    std::vector<ItemRef> items_host;     // item table (item table order)
     // Split-BF16 tensor-core panels of the dense part (SpMM, built lazily).
     void *tc = nullptr;
     // SpMM scratch, grown on demand by the first call that needs more.
@@ -60,5 +70,5 @@ struct sable_plan {
 
 namespace sable {
 int plan_upload(sable_plan *p, const Layout &L);
-SpmvArgs spmv_args(const sable_plan *p, const float *x, float *y, int64_t *cycles);
+LaunchArgs spmv_args(const sable_plan *p, const float *x, float *y, int64_t *cycles);
 }  // namespace sable

@@ -1,92 +1,117 @@
 // Internal layout shared by the host plan builder and the device kernels.
 //
-// Device layout of one plan (all in HBM, built once by sable_plan_create):
+// Device layout of one plan (HBM, built once by sable_plan_create):
 //
 //   tiles     A block row of height <= row_tile is one tile; a taller block
 //             row is cut into near-equal tiles.  Empty block rows become
 //             zero tiles so that every output row is written by exactly one
 //             tile (no memset of y is ever needed).
-//   panel     float4[]  For each tile, the columns of its dense blocks (bindx
-//             order) are concatenated and padded to a multiple of 4; element
-//             (q, i) = A[i, 4q .. 4q+3] of quad q, row i, stored at q*h + i.
-//             A tile's panel is therefore one contiguous float4 stream in
-//             which consecutive threads read consecutive 16-byte words while
-//             every thread keeps a fixed row.
-//   sparse    uint2[]   The CSR entries of the tile's rows, in CSR order:
-//             .x = value bits, .y = column | local_row << 25.  8 bytes per
-//             nonzero, no row pointer array.
-//   runs      int4[]    x gather runs of a work item: (dst, col0, len, 0):
-//             xs[dst + k] = x[col0 + k] for k < len.
-//   chunks    Chunk[]   Work items of at most ~chunk_bytes of matrix data;
-//             a tile split over several chunks reduces its partial sums in a
-//             fixed order in the last-arriving CTA (deterministic).
+//   items     A tile's work is cut into items of at most ~item_bytes.  Each
+//             item is one contiguous, 16-byte aligned record:
+//
+//               ItemHeader                       64 bytes
+//               xcol   int32[4*nq]               x column of each panel column
+//               panel  float4[nq*h]              quad panel: (q, i) = A[i, 4q..4q+3]
+//               rowptr int32[h+1] (16 B padded)  CSR row starts, item-relative
+//               csr    uint2[ns]  (16 B padded)  (value bits, column)
+//
+//             The dense blocks of a tile are concatenated column by column
+//             (bindx order) and padded to a multiple of 4 columns; a panel
+//             quad holds 4 columns of one row, so consecutive threads read
+//             consecutive 16-byte words while every thread keeps its row.
+//             One TMA bulk copy brings a whole item into shared memory.
+//   table     int64 offset / bytes of each item, and per persistent CTA the
+//             [begin, end) range of its items (greedy LPT over item bytes).
+//   Split tiles publish per-item partial row sums; the last-arriving CTA
+//   adds them in item order (deterministic, no atomics on y).
 #pragma once
 #include <stdint.h>
 
 #define SABLE_MAX_ROW_TILE 128
-#define SABLE_COL_BITS 25
-#define SABLE_COL_MASK ((1u << SABLE_COL_BITS) - 1u)
-#define SABLE_MAX_COLS (1 << SABLE_COL_BITS)
-#define SABLE_MAX_CHUNK_QUADS 1024   // xs staging: 16 KB of shared memory
-#define SABLE_MAX_CHUNK_RUNS 256     // run table: 4 KB of shared memory
 #define SABLE_THREADS 256
-#define SABLE_VT 4                   // virtual row-threads per thread (dense SpMV)
+#define SABLE_NWARP (SABLE_THREADS / 32)
+#define SABLE_MAX_ITEM_BYTES 98304   // record bytes; bounds a TMA staging buffer
+#define SABLE_WSTAGES 2              // TMA ring depth of a persistent warp worker
+#define SABLE_ITEMS_ITEM_BYTES 32768 // default item size, one CTA per item
+#define SABLE_WARP_ITEM_BYTES 8192   // default item size, warp workers
+#define SABLE_SCHEDULE_ITEMS 0
+#define SABLE_SCHEDULE_PERSISTENT 1
 
-struct __align__(16) Chunk {
-    int64_t panel_f4;   // float4 index of the chunk's first panel word
-    int64_t sp0;        // first sparse entry
-    int64_t part_base;  // float offset of the tile's partial slots (split tiles)
+struct __align__(16) ItemHeader {
     int32_t row0;       // first output row of the tile
     int32_t h;          // rows of the tile
-    int32_t nq;         // dense quads in this chunk
-    int32_t ns;         // sparse entries in this chunk
-    int32_t run0;       // first x run
-    int32_t nrun;       // x runs
-    int32_t tile;       // split-tile counter index, -1 for a single-chunk tile
-    int32_t kidx;       // position of the chunk within its tile
-    int32_t nchunk;     // chunks of the tile
-    int32_t pad;
+    int32_t nq;         // panel quads in this item
+    int32_t ns;         // CSR entries in this item
+    int32_t xcol_off;   // byte offsets of the record's parts
+    int32_t panel_off;
+    int32_t rp_off;
+    int32_t csr_off;
+    int32_t tile;       // split-tile counter index, -1 for a single-item tile
+    int32_t kidx;       // position of the item within its tile
+    int32_t nitem;      // items of the tile
+    int32_t g;          // lanes per CSR row (4, 8, 16 or 32)
+    int64_t part_base;  // float offset of the tile's partial slots (split tiles)
+    int32_t bytes;      // record bytes (multiple of 16)
+    int32_t mat;        // matrix index inside a batch (0 for a single plan)
 };
-static_assert(sizeof(Chunk) == 64, "Chunk must stay 64 bytes");
+static_assert(sizeof(ItemHeader) == 64, "ItemHeader must stay 64 bytes");
 
-struct SpmvArgs {
-    const Chunk *chunks;
-    const float4 *panel;
-    const uint2 *sparse;
-    const int4 *runs;
+struct ItemRef {        // item table entry
+    int64_t off;        // byte offset of the record
+    int32_t bytes;      // record bytes
+    int32_t cost;       // scheduling weight (bytes or SpMM work)
+};
+
+// Entry of a warp worker's list (persistent schedule).  Consecutive items of
+// one tile form a part; a warp accumulates over the items of a part in
+// registers and writes the rows once, at the part's last item.
+#define SABLE_PART_FIRST 1
+#define SABLE_PART_LAST 2
+struct WorkRef {
+    int64_t off;        // byte offset of the record
+    int64_t part_base;  // float offset of the tile's part partials (multi-part tiles)
+    int32_t bytes;      // record bytes
+    int32_t flags;      // SABLE_PART_FIRST / SABLE_PART_LAST
+    int32_t part;       // index of the part within its tile
+    int32_t nparts;     // parts of the tile
+    int32_t split;      // counter index of a multi-part tile, -1 otherwise
+    int32_t pad[3];
+};
+static_assert(sizeof(WorkRef) == 48, "WorkRef must stay 48 bytes");
+
+// One matrix of a launch: its operand / result and (SpMM) width.
+struct MatIO {
     const float *x;
     float *y;
-    float *partial;     // split-tile partial sums
+    float *partial;     // split-tile partial sums of this matrix (per item)
     int *counters;      // split-tile arrival counters (self-resetting)
-    int64_t *ns_out;    // per-chunk durations (timed variant) or nullptr
-    int n_chunks;
-    int *work_counter;  // persistent variant: next chunk to take (self-resetting)
-    int *done_counter;  // persistent variant: CTAs finished (self-resetting)
-};
-
-struct SpmmArgs {
-    const Chunk *chunks;
-    const float4 *panel;
-    const uint2 *sparse;
-    const int4 *runs;
-    const float *X;
-    float *Y;
-    float *partial;
-    int *counters;
-    int64_t *ns_out;
+    float *ppartial;    // multi-part tile partial sums (persistent schedule)
+    int *pcounters;     // multi-part tile arrival counters (self-resetting)
     int64_t ldx, ldy;
-    int N;              // total width
-    int nt;             // width handled by one work item (power of two, <= 128)
-    int n_slices;       // ceil(N / nt)
-    int n_chunks;
-    int64_t part_stride; // floats of partial scratch per N-slice
+    int32_t N;          // 1 for SpMV
+    int32_t pad;
 };
 
-// Host-side launchers implemented in the .cu files.
+struct LaunchArgs {
+    const unsigned char *records;
+    const ItemRef *items;
+    const WorkRef *work;    // persistent: worker lists, concatenated
+    const int *cta_begin;   // persistent: worker w's entries are [cta_begin[w], cta_begin[w+1])
+    const MatIO *mats;      // per matrix (batch); nullptr: every item uses mat0
+    MatIO mat0;
+    int64_t *cycles;        // per-item SM cycles (timed variant) or nullptr
+    int *error;             // set to 1 when a bounded device wait runs out
+    int n_items;
+    int stage_bytes;        // TMA staging bytes per stage (>= largest record)
+    int xg_floats;          // x-gather buffer floats (>= 4 nq + ns of any item)
+};
+
 namespace sable {
-int launch_spmv(const SpmvArgs &a, int smem_bytes, bool timed, void *stream);
-int launch_spmm_fp32(const SpmmArgs &a, int smem_bytes, bool timed, void *stream);
-int spmv_smem_bytes(int max_quads, int max_runs);
-int spmm_smem_bytes(int nt, int max_quads, int max_runs, int row_tile);
+int launch_spmv_items(const LaunchArgs &a, bool timed, void *stream);
+int launch_spmv_warps(const LaunchArgs &a, int n_workers, void *stream);
+int spmv_items_smem(int stage_bytes, int xg_floats);
+int spmv_warp_smem(int stage_bytes, int xg_floats);
+int spmv_warp_workers_per_sm(int stage_bytes, int xg_floats);
+int launch_spmm_fp32(const LaunchArgs &a, int N, int nt, int64_t part_stride, bool timed, void *stream);
 const char *cuda_error_string(int err);
 }  // namespace sable

@@ -25,11 +25,14 @@ def _stream_handle(stream) -> int | None:
 class Plan:
     """GPU plan of one compressed VBR matrix."""
 
+    SCHEDULES = {"items": 0, "persistent": 1}
+
     def __init__(self, comp: Compressed, row_tile: int = 0, chunk_bytes: int = 0, spmm_tc: bool = False,
-                 device: int | None = None):
+                 device: int | None = None, schedule: str = "items"):
         lib = _lib.load()
         desc, keep = _lib.make_desc(comp)
-        opts = _lib.PlanOpts(int(row_tile), int(chunk_bytes), int(bool(spmm_tc)), -1 if device is None else int(device))
+        opts = _lib.PlanOpts(int(row_tile), int(chunk_bytes), int(bool(spmm_tc)), -1 if device is None else int(device),
+                             self.SCHEDULES[schedule])
         h = ctypes.c_void_p()
         _lib.check(lib.sable_plan_create(ctypes.byref(desc), ctypes.byref(opts), ctypes.byref(h)), "sable_plan_create")
         del keep
@@ -39,6 +42,7 @@ class Plan:
         self.spmm_tc = bool(spmm_tc)
         self.row_tile = row_tile
         self.chunk_bytes = chunk_bytes
+        self.schedule = schedule
 
     @property
     def handle(self) -> int:
@@ -50,6 +54,10 @@ class Plan:
         s = _lib.PlanStats()
         _lib.check(_lib.load().sable_plan_get_stats(self.handle, ctypes.byref(s)), "sable_plan_get_stats")
         return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def check(self, stream=None) -> None:
+        """Raise if a bounded device wait ran out in an earlier launch."""
+        _lib.check(_lib.load().sable_plan_check(self.handle, _stream_handle(stream)), "sable_plan_check")
 
     def chunk_tiles(self) -> np.ndarray:
         n = self.stats()["n_chunks"]

@@ -85,13 +85,13 @@ def test_block_features_match_numpy():
 def dry_run(comp, row_tile=0, chunk_bytes=0):
     desc, keep = _lib.make_desc(comp)
     st = _lib.PlanStats()
-    opts = _lib.PlanOpts(row_tile, chunk_bytes, 0, -1)
+    opts = _lib.PlanOpts(row_tile, chunk_bytes, 0, -1, 0)
     _lib.check(_lib.load().sable_plan_dry_run(ctypes.byref(desc), ctypes.byref(opts), ctypes.byref(st)), "dry_run")
     return {k: getattr(st, k) for k, _ in st._fields_}
 
 
 @pytest.mark.parametrize("row_tile", [128, 64, 17, 1])
-@pytest.mark.parametrize("chunk_bytes", [0, 1024, 256])
+@pytest.mark.parametrize("chunk_bytes", [0, 4096, 6000, 32768])
 def test_layout_builder_edge_shapes(row_tile, chunk_bytes):
     """Tall rows, width/height-1 partitions, empty rows, tiny work items:
     the builder's own bounds check (check_layout) passes and every stored

@@ -58,7 +58,7 @@ def test_widths(cuda, N):
     assert r["pass"], r
 
 
-@pytest.mark.parametrize("chunk_bytes", [0, 2048])
+@pytest.mark.parametrize("chunk_bytes", [0, 4096])
 @pytest.mark.parametrize("tc", [False, True])
 def test_split_tiles_and_edges(cuda, chunk_bytes, tc):
     m = random_vbr(6, [1, 300, 64, 2, 100], [1, 250, 3, 64, 77, 2, 31], 0.8)

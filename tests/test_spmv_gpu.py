@@ -78,8 +78,9 @@ def test_spmv1000_vs_reference_c(golden, cuda, case, density):
 
 
 @pytest.mark.parametrize("row_tile", [128, 64, 17])
-@pytest.mark.parametrize("chunk_bytes", [0, 1024])
-def test_edge_shapes(cuda, row_tile, chunk_bytes):
+@pytest.mark.parametrize("chunk_bytes", [0, 4096])
+@pytest.mark.parametrize("schedule", ["persistent", "items"])
+def test_edge_shapes(cuda, row_tile, chunk_bytes, schedule):
     """Tall block rows (tile splits), width-1 / height-1 partitions, empty
     block rows, tiny work items (split tiles, last-arriver reduction)."""
     rs = [1, 300, 5, 1, 64, 129, 7, 2, 40]
@@ -88,7 +89,7 @@ def test_edge_shapes(cuda, row_tile, chunk_bytes):
     x = synth.vector(m.n_cols, 8)
     rng = np.random.default_rng(9)
     dense = rng.random(m.n_blocks) < 0.5
-    plan, comp, y_ref, yabs = plan_and_ref(m, dense, x, row_tile=row_tile, chunk_bytes=chunk_bytes)
+    plan, comp, y_ref, yabs = plan_and_ref(m, dense, x, row_tile=row_tile, chunk_bytes=chunk_bytes, schedule=schedule)
     y = run(plan, x)
     r = oracle.report(y, y_ref, yabs)
     assert r["pass"], r
@@ -120,7 +121,7 @@ def test_deterministic_and_host_entry(cuda):
     m = synth.spmv_1000()
     x = synth.vector(m.n_cols, 21)
     rng = np.random.default_rng(22)
-    plan, comp, y_ref, yabs = plan_and_ref(m, rng.random(m.n_blocks) < 0.5, x, chunk_bytes=2048)
+    plan, comp, y_ref, yabs = plan_and_ref(m, rng.random(m.n_blocks) < 0.5, x, chunk_bytes=4096)
     xd = torch.as_tensor(x).cuda()
     y1 = plan.spmv(xd).cpu().numpy()
     y2 = plan.spmv(xd).cpu().numpy()
@@ -128,6 +129,7 @@ def test_deterministic_and_host_entry(cuda):
     y3 = plan.spmv_host(x)
     np.testing.assert_array_equal(y1, y3)
     assert oracle.report(y1, y_ref, yabs)["pass"]
+    plan.check()  # no bounded device wait ran out
 
 
 def test_spmv_100k_full_size(cuda):
@@ -140,8 +142,9 @@ def test_spmv_100k_full_size(cuda):
     bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
     nnz = convert.block_nnz(m.val, bt)
     cheaper_dense = 4 * bt.size <= 8 * nnz + 4 * (bt.h + 1)
-    for dense in (cheaper_dense, np.zeros(m.n_blocks, bool)):
-        plan, comp, y_ref, yabs = plan_and_ref(m, dense, x)
+    for dense, schedule in ((cheaper_dense, "persistent"), (np.zeros(m.n_blocks, bool), "persistent"),
+                            (cheaper_dense, "items")):
+        plan, comp, y_ref, yabs = plan_and_ref(m, dense, x, schedule=schedule)
         y = run(plan, x)
         r = oracle.report(y, y_ref, yabs)
         assert r["pass"], r
