@@ -393,7 +393,7 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
     if (!out) return fail(SABLE_ERR_ARG, "null output pointer");
     const int row_tile = opts && opts->row_tile ? opts->row_tile : SABLE_MAX_ROW_TILE;
     const int chunk_bytes = opts && opts->chunk_bytes ? opts->chunk_bytes
-                            : (opts && opts->schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES : SABLE_WARP_ITEM_BYTES);
+                            : (!opts || opts->schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES : SABLE_WARP_ITEM_BYTES);
     if (row_tile < 1 || row_tile > SABLE_MAX_ROW_TILE) return fail(SABLE_ERR_ARG, "row_tile %d outside 1..128", row_tile);
     if (chunk_bytes < 4096 || chunk_bytes > SABLE_MAX_ITEM_BYTES * 4 / 5) return fail(SABLE_ERR_ARG, "chunk_bytes outside range");
     int rc = validate_vbrc(desc);

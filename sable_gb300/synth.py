@@ -66,6 +66,8 @@ def random_splits(rng, n: int, parts: int) -> np.ndarray:
 def sizes_with_sum(rng, parts: int, lo: int, hi: int, total: int) -> np.ndarray:
     """`parts` sizes drawn U[lo, hi], then random unit steps (decrements of
     sizes > lo, or increments of sizes < hi) until they sum to `total`."""
+    if not parts * lo <= total <= parts * hi:
+        raise ValueError(f"{parts} sizes in [{lo}, {hi}] cannot sum to {total}")
     s = rng.integers(lo, hi + 1, size=parts).astype(np.int64)
     diff = int(s.sum()) - total
     while diff != 0:

@@ -163,3 +163,8 @@ def test_oracle_planted_mistake_is_caught():
     c.val[len(c.val) // 2] += 0.5
     y2, _ = oracle.spmv_vbrc(c, x)
     assert not oracle.report(y2, y, ya)["pass"]
+
+
+def test_partition_sizes_infeasible_total_raises():
+    with pytest.raises(ValueError):
+        synth.sizes_with_sum(np.random.default_rng(0), 30, 20, 80, 3000)
