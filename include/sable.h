@@ -123,6 +123,23 @@ int sable_spmm(sable_plan *plan, const float *X_dev, int64_t ldx, float *Y_dev, 
                int32_t N, void *stream);
 int sable_spmm_host(sable_plan *plan, const float *X_host, float *Y_host, int32_t N, void *stream);
 
+/* SpMM that allocates no memory (no counterpart in the reference).
+ * Same result and arguments as sable_spmm on the FP32 path, for callers that
+ * cannot let a library allocate device memory during a call: code running
+ * while a CUDA graph is being captured, runtimes whose pool allocator owns
+ * all device memory, real-time loops that must not block on cudaMalloc.
+ * sable_spmm allocates split-tile scratch on its first call at a given width;
+ * this entry point uses a fixed scratch array compiled into the library
+ * instead (8 MiB of partial sums + 256 KiB of counters, held by every device
+ * that loads the library until the process exits) and returns
+ * SABLE_ERR_UNSUPPORTED when a plan at width N needs more than that.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array: calls that may overlap on the GPU (other
+ * streams, other host threads) race and must be serialised by the caller. */
+int sable_spmm_noalloc(sable_plan *plan, const float *X_dev, int64_t ldx, float *Y_dev, int64_t ldy,
+                       int32_t N, void *stream);
+
 /* Per-work-item device time (SM clock cycles) of one SpMV / SpMM launch,
  * written to cycles_dev[n_chunks] (SpMM: [n_slices][n_chunks]); used to
  * time blocks for the learned block model (the GPU counterpart of

@@ -67,6 +67,7 @@ SIGNATURES = {
     "sable_spmv_host": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "sable_spmm": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_void_p]),
     "sable_spmm_host": (c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p]),
+    "sable_spmm_noalloc": (c_int, [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_int32, c_void_p]),
     "sable_spmv_timed": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "sable_spmm_timed": (c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p]),
     "sable_plan_chunk_tiles": (c_int, [c_void_p, c_void_p]),
