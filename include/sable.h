@@ -76,13 +76,21 @@ typedef struct sable_plan_opts {
     int32_t row_tile;     /* rows per tile, 1..128 (0: 128)                    */
     int32_t chunk_bytes;  /* target matrix bytes per work item, 256..98304
                              (0: 32768)                                        */
-    int32_t spmm_tc;      /* 1: dense blocks of SpMM with N >= 32 run as
-                             split-BF16 on the tensor cores                     */
+    int32_t spmm_tc;      /* dense blocks of SpMM with N >= 32 on the tensor
+                             cores as split BF16 with FP32 accumulation:
+                             SABLE_TC_SPLIT2 (1): hi+lo, three products,
+                               per-product error <= 3*2^-16 |a||b|;
+                             SABLE_TC_SPLIT3 (2): hi+mid+lo, six products,
+                               FP32-level error.  0: FP32 CUDA cores.          */
     int32_t device;       /* CUDA device ordinal (-1: current)                 */
     int32_t schedule;     /* 0: one CTA per work item (TMA-staged record);
                              1: persistent warp workers over an LPT schedule
                              of tile parts, each with a private TMA ring       */
 } sable_plan_opts;
+
+#define SABLE_TC_OFF    0
+#define SABLE_TC_SPLIT2 1
+#define SABLE_TC_SPLIT3 2
 
 /* Sizes of a built plan (for byte accounting and tests). */
 typedef struct sable_plan_stats {

@@ -155,12 +155,12 @@ def _density_mask(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density: int, 
 
 
 def gen_single_threaded_spmm(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density: int, dir_name: str,
-                             filename: str, vbr_dir: str, spmm_tc: bool = True, **plan_opts) -> PlanRecord:
+                             filename: str, vbr_dir: str, spmm_tc="split3", **plan_opts) -> PlanRecord:
     bt, dense = _density_mask(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density)
     comp = compress(np.asarray(val, dtype=np.float32), rpntr, cpntr, indx, bindx, bpntrb, bpntre, dense, bt=bt)
     plan = Plan(comp, spmm_tc=spmm_tc, **plan_opts)
     rec = PlanRecord(plan, "spmm", comp.n_rows, comp.n_cols, 1,
-                     {"vbr_dir": os.path.abspath(vbr_dir), "density": density, "threads": 1, "spmm_tc": bool(spmm_tc)})
+                     {"vbr_dir": os.path.abspath(vbr_dir), "density": density, "threads": 1, "spmm_tc": plan.spmm_tc})
     _register(dir_name, filename, rec)
     return rec
 
@@ -214,7 +214,7 @@ def vbr_spmv_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: i
     return time.time_ns() // 1_000 - t1
 
 
-def vbr_spmm_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: int, spmm_tc: bool = True,
+def vbr_spmm_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: int, spmm_tc="split3",
                           **plan_opts) -> int:
     val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(os.path.join(vbr_dir, filename + ".vbr"))
     t1 = time.time_ns() // 1_000

@@ -166,8 +166,6 @@ static int ensure_spmm_scratch(sable_plan *p, int nt, int n_slices) {
     return SABLE_OK;
 }
 
-int spmm_tc_run(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_t ldy, int N, int64_t *cycles,
-                void *stream, bool *handled);
 void spmm_tc_free(sable_plan *p);
 
 static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_t ldy, int N, int64_t *cycles,
@@ -179,11 +177,6 @@ static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_
     if (((uintptr_t)X & 15) || ((uintptr_t)Y & 15)) return fail(SABLE_ERR_UNSUPPORTED, "SpMM operands must be 16-byte aligned");
     int rc = set_device(p->device);
     if (rc) return rc;
-    if (p->spmm_tc && N >= 32) {
-        bool handled = false;
-        rc = spmm_tc_run(p, X, ldx, Y, ldy, N, cycles, stream, &handled);
-        if (rc || handled) return rc;
-    }
     const int nt = pick_nt(N);
     const int n_slices = (N + nt - 1) / nt;
     rc = ensure_spmm_scratch(p, nt, n_slices);
@@ -205,7 +198,10 @@ static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_
     a.n_items = (int)p->n_items;
     a.stage_bytes = p->max_item_bytes;
     const int64_t part_stride = p->n_partial * nt;
-    int e = launch_spmm_fp32(a, N, nt, part_stride, cycles != nullptr, stream);
+    // dense blocks on the tensor cores (split-BF16) when enabled and N >= 32
+    const bool tc = p->spmm_tc && N >= 32;
+    int e = tc ? launch_spmm_tc(a, N, nt, p->spmm_tc == SABLE_TC_SPLIT3 ? 3 : 2, part_stride, cycles != nullptr, stream)
+               : launch_spmm_fp32(a, N, nt, part_stride, cycles != nullptr, stream);
     (void)n_slices;
     if (e) return cuda_fail((cudaError_t)e, "spmm launch");
     return SABLE_OK;

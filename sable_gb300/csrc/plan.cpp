@@ -379,6 +379,10 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
         return fail(SABLE_ERR_ARG, "schedule %d unknown", o.schedule);
     }
     p->schedule = o.schedule;
+    if (o.spmm_tc < SABLE_TC_OFF || o.spmm_tc > SABLE_TC_SPLIT3) {
+        delete p;
+        return fail(SABLE_ERR_ARG, "spmm_tc %d unknown", o.spmm_tc);
+    }
     p->spmm_tc = o.spmm_tc;
     Layout L;
     rc = build_layout(desc, row_tile, chunk_bytes, L);

@@ -113,5 +113,7 @@ int spmv_items_smem(int stage_bytes, int xg_floats);
 int spmv_warp_smem(int stage_bytes, int xg_floats);
 int spmv_warp_workers_per_sm(int stage_bytes, int xg_floats);
 int launch_spmm_fp32(const LaunchArgs &a, int N, int nt, int64_t part_stride, bool timed, void *stream);
+// terms = 2: three BF16 products (hi+lo split); 3: six products (hi+mid+lo).
+int launch_spmm_tc(const LaunchArgs &a, int N, int nt, int terms, int64_t part_stride, bool timed, void *stream);
 const char *cuda_error_string(int err);
 }  // namespace sable
