@@ -181,30 +181,38 @@ int sable_batch_destroy(sable_batch *batch);
 int sable_block_features(const sable_vbrc_desc *desc, int32_t N, float *feat_out);
 
 /*
- * Block cost model: MLP 6 -> 64 -> 64 -> 2 (ReLU), FP32, predicting the log
- * device time of the dense and of the sparse form of a block.  It replaces
+ * Block cost model: MLP 6 -> 64 -> 64 -> 2 (ReLU), FP32, predicting log2 of
+ * the device time (SM cycles) of the dense and of the sparse form of a block;
+ * a block is stored dense iff its first output is the smaller.  It replaces
  * the pickled RandomForest threshold (models/density_threshold_spmv.pkl,
- * used at utils/convert_real_to_vbr.py:20,58).  Training and inference run
- * on the device in this library's own kernels.
- * Parameter order in flat buffers: W1[64x6], b1[64], W2[64x64], b2[64],
- * W3[2x64], b3[2] (row-major, out x in) = 4674 floats.
+ * loaded at utils/convert_real_to_vbr.py:20 and queried per block at :58).
+ * Training and inference run on the device in this library's own kernels.
+ * Features are the rows of sable_block_features; the kernels transform them
+ * to log2(1 + f) (all but density) and then to (g - mean) / std.
+ * Parameter order in flat buffers (row-major, out x in):
+ *   W1[64x6], b1[64], W2[64x64], b2[64], W3[2x64], b3[2] = 4738 floats.
  */
-#define SABLE_MLP_NPARAMS 4674
-int sable_mlp_create(sable_mlp **out);
+#define SABLE_MLP_NPARAMS 4738
+int sable_mlp_create(sable_mlp **out);            /* on the current device, params 0 */
 int sable_mlp_destroy(sable_mlp *m);
+/* Loads parameters and resets the optimiser state (Adam moments, step). */
 int sable_mlp_set_params(sable_mlp *m, const float *params_host);
 int sable_mlp_get_params(const sable_mlp *m, float *params_host);
-/* Feature normalisation: z = (f - mean) / std applied in-kernel. */
+/* Feature normalisation of the transformed features; std6[i] > 0. */
 int sable_mlp_set_norm(sable_mlp *m, const float *mean6, const float *std6);
-/* out_dev[n x 2] = MLP(feat_dev[n x 6]). */
+/* out_dev[n x 2] = MLP(feat_dev[n x 6]); n = 0 is a no-op. */
 int sable_mlp_infer(sable_mlp *m, const float *feat_dev, int32_t n, float *out_dev, void *stream);
-/* Mean squared error loss and gradient of all parameters over a batch
- * (grad_dev[SABLE_MLP_NPARAMS], loss_dev[1]); no parameter update. */
+/* Loss L = 1/(2n) sum (out - target)^2 over the n x 2 outputs and its
+ * gradient with respect to every parameter (grad_dev[SABLE_MLP_NPARAMS],
+ * loss_dev[1] or NULL); no parameter update.  Deterministic: the same inputs
+ * give bit-identical results. */
 int sable_mlp_loss_grad(sable_mlp *m, const float *feat_dev, const float *target_dev, int32_t n,
                         float *grad_dev, float *loss_dev, void *stream);
-/* One Adam step on a batch (loss_dev may be NULL). */
-int sable_mlp_train_step(sable_mlp *m, const float *feat_dev, const float *target_dev, int32_t n,
-                         float lr, float *loss_dev, void *stream);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on a batch of n samples:
+ * sample s is row idx_dev[s] of feat_dev / target_dev (idx_dev NULL: row s).
+ * loss_dev (may be NULL) receives the batch loss before the step. */
+int sable_mlp_train_step(sable_mlp *m, const float *feat_dev, const float *target_dev, const int32_t *idx_dev,
+                         int32_t n, float lr, float *loss_dev, void *stream);
 
 const char *sable_strerror(int code);
 const char *sable_last_error(void);

@@ -18,7 +18,7 @@ SABLE_ERR_NOMEM = -3
 SABLE_ERR_UNSUPPORTED = -4
 SABLE_ERR_TIMEOUT = -5
 SABLE_ERR_ARG = -6
-MLP_NPARAMS = 4674
+MLP_NPARAMS = 4738
 
 
 class SableError(RuntimeError):
@@ -82,7 +82,7 @@ SIGNATURES = {
     "sable_mlp_set_norm": (c_int, [c_void_p, c_void_p, c_void_p]),
     "sable_mlp_infer": (c_int, [c_void_p, c_void_p, c_int32, c_void_p, c_void_p]),
     "sable_mlp_loss_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p]),
-    "sable_mlp_train_step": (c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_float, c_void_p, c_void_p]),
+    "sable_mlp_train_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_float, c_void_p, c_void_p]),
     "sable_strerror": (c_char_p, [c_int]),
     "sable_last_error": (c_char_p, []),
     "sable_version": (c_char_p, []),

@@ -185,6 +185,129 @@ class MLPModel:
             pass
 
 
+def transform_features(feats: np.ndarray) -> np.ndarray:
+    """The kernels' feature transform before normalisation: log2(1 + f) for
+    every feature but density (column 3), which is kept as is."""
+    f = np.asarray(feats, dtype=np.float64)
+    g = np.log2(1.0 + f)
+    g[:, 3] = f[:, 3]
+    return g
+
+
+def init_params(seed: int = 0) -> np.ndarray:
+    """He-uniform weights (bound sqrt(6 / fan_in)), zero biases, flat order
+    W1 b1 W2 b2 W3 b3."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for out_f, in_f in ((64, 6), (64, 64), (2, 64)):
+        lim = np.sqrt(6.0 / in_f)
+        parts += [rng.uniform(-lim, lim, size=out_f * in_f), np.zeros(out_f)]
+    p = np.concatenate(parts).astype(np.float32)
+    assert p.size == _lib.MLP_NPARAMS
+    return p
+
+
+def byte_rule(feats: np.ndarray) -> np.ndarray:
+    """Dense iff the dense panel moves no more bytes than the CSR form:
+    4 h w <= 8 nnz + 4 (h + 1)."""
+    f = np.asarray(feats, dtype=np.float64)
+    return 4 * f[:, 0] * f[:, 1] <= 8 * f[:, 2] + 4 * (f[:, 0] + 1)
+
+
+def regret(dense_choice: np.ndarray, t_dense: np.ndarray, t_sparse: np.ndarray) -> float:
+    """sum of the chosen forms' times over the sum of the per-block best, - 1."""
+    chosen = np.where(np.asarray(dense_choice, bool), t_dense, t_sparse)
+    best = np.minimum(t_dense, t_sparse)
+    return float(chosen.sum() / best.sum() - 1.0)
+
+
+class MLPTrainer:
+    """Adam training of the block cost model on the device through
+    sable_mlp_train_step (forward, backward and update in libsable's kernels).
+    Device memory and the sample shuffle are PyTorch tensors."""
+
+    def __init__(self, params: np.ndarray, mean: np.ndarray, std: np.ndarray, device: int = 0):
+        import torch
+        self.lib = _lib.load()
+        self.dev = torch.device("cuda", device)
+        torch.cuda.set_device(self.dev)
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.sable_mlp_create(ctypes.byref(h)), "sable_mlp_create")
+        self._h = h
+        self.mean = np.ascontiguousarray(mean, dtype=np.float32)
+        self.std = np.ascontiguousarray(std, dtype=np.float32)
+        self.set_params(params)
+        _lib.check(self.lib.sable_mlp_set_norm(h, self.mean.ctypes.data, self.std.ctypes.data), "sable_mlp_set_norm")
+
+    def set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.size == _lib.MLP_NPARAMS
+        _lib.check(self.lib.sable_mlp_set_params(self._h, p.ctypes.data), "sable_mlp_set_params")
+
+    def params(self) -> np.ndarray:
+        out = np.empty(_lib.MLP_NPARAMS, dtype=np.float32)
+        _lib.check(self.lib.sable_mlp_get_params(self._h, out.ctypes.data), "sable_mlp_get_params")
+        return out
+
+    def _stream(self):
+        import torch
+        return torch.cuda.current_stream(self.dev).cuda_stream
+
+    def loss_grad(self, feat, target):
+        """(loss, grad) of a device batch; both device tensors."""
+        import torch
+        grad = torch.empty(_lib.MLP_NPARAMS, dtype=torch.float32, device=self.dev)
+        loss = torch.empty(1, dtype=torch.float32, device=self.dev)
+        _lib.check(self.lib.sable_mlp_loss_grad(self._h, feat.data_ptr(), target.data_ptr(), int(feat.shape[0]),
+                                                grad.data_ptr(), loss.data_ptr(), self._stream()),
+                   "sable_mlp_loss_grad")
+        return loss, grad
+
+    def step(self, feat, target, idx, lr: float, loss=None) -> None:
+        _lib.check(self.lib.sable_mlp_train_step(self._h, feat.data_ptr(), target.data_ptr(),
+                                                 None if idx is None else idx.data_ptr(),
+                                                 int(feat.shape[0] if idx is None else idx.shape[0]), float(lr),
+                                                 None if loss is None else loss.data_ptr(), self._stream()),
+                   "sable_mlp_train_step")
+
+    def fit(self, feats: np.ndarray, targets: np.ndarray, epochs: int = 40, batch: int = 2048, lr: float = 3e-3,
+            lr_final: float = 3e-4, seed: int = 0, log=None, center_output: bool = True) -> list[float]:
+        """Mini-batch Adam over (feats, targets) with a per-epoch shuffle and a
+        geometric learning-rate decay from lr to lr_final; returns the mean
+        batch loss of each epoch.  center_output starts the output biases at
+        the mean target (Adam moves a parameter by about lr per step, too
+        slowly to travel to log2 cycles from 0)."""
+        import torch
+        if center_output:
+            p = self.params()
+            p[-2:] = np.asarray(targets, np.float64).mean(0)
+            self.set_params(p)
+        f = torch.as_tensor(np.ascontiguousarray(feats, dtype=np.float32), device=self.dev)
+        t = torch.as_tensor(np.ascontiguousarray(targets, dtype=np.float32), device=self.dev)
+        n = f.shape[0]
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        losses = torch.zeros(max(1, (n + batch - 1) // batch), dtype=torch.float32, device=self.dev)
+        hist = []
+        for ep in range(epochs):
+            rate = lr * (lr_final / lr) ** (ep / max(1, epochs - 1))
+            perm = torch.randperm(n, generator=g).to(torch.int32).to(self.dev)
+            nb = 0
+            for b0 in range(0, n, batch):
+                self.step(f, t, perm[b0:b0 + batch], rate, losses[nb:nb + 1])
+                nb += 1
+            hist.append(float(losses[:nb].mean()))
+            if log:
+                log(f"epoch {ep} lr {rate:.2e} loss {hist[-1]:.5f}")
+        return hist
+
+    def __del__(self):
+        try:
+            if self._h:
+                self.lib.sable_mlp_destroy(self._h)
+        except Exception:
+            pass
+
+
 def default_model():
     """The learned model when its weights and a GPU are present, else the
     reference RandomForest table."""
