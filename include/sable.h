@@ -160,19 +160,40 @@ int sable_plan_chunk_tiles(const sable_plan *plan, int64_t *tile_of_chunk);
 
 /*
  * Batch: many plans (matrices) executed by one persistent kernel over a
- * shared work queue sorted by class and size.  No reference counterpart (the
- * reference times matrices one process at a time); widths[i] = 1 runs SpMV on
- * plan i, widths[i] = N > 1 runs SpMM of width N.
+ * shared work queue.  No reference counterpart (the reference times one
+ * matrix per process).  widths[i] = 1 runs SpMV on plan i; widths[i] = N > 1
+ * (N % 4 == 0) runs SpMM of width N, on the tensor cores when plan i was
+ * created with spmm_tc and N >= 32.  Work units are (item, N-slice) pairs of
+ * every plan, sorted by class (split-BF16 SpMM, FP32 SpMM, SpMV) and, within
+ * a class, by size, largest first; persistent CTAs take units in that order
+ * from an atomic queue head, and every SpMV record is prefetched by TMA while
+ * the previous unit is computed.  The batch copies the plans' records; the
+ * plans may be destroyed after sable_batch_create.
  */
 typedef struct sable_batch_opts {
-    int32_t ctas_per_sm;  /* persistent CTAs per SM (0: from occupancy)       */
-    int32_t use_graph;    /* 1: capture the launch in a CUDA graph            */
+    int32_t ctas_per_sm;  /* persistent CTAs per SM (0: as many as fit)       */
+    int32_t use_graph;    /* 1: sable_batch_run replays a CUDA graph of the
+                             queue reset and the kernel launch                 */
 } sable_batch_opts;
+
+typedef struct sable_batch_info {
+    int32_t n_mats;
+    int32_t n_ctas;           /* persistent CTAs of the launch               */
+    int64_t n_units;          /* work units in the queue                     */
+    int64_t device_bytes;     /* records, tables and scratch of the batch    */
+    int32_t smem_bytes;       /* dynamic shared memory per CTA               */
+    int32_t stage_bytes;      /* TMA staging bytes per SpMV stage            */
+} sable_batch_info;
 
 int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t *widths,
                        const sable_batch_opts *opts, sable_batch **out);
-/* x_devs[i] / y_devs[i]: operand and result of plan i (X/Y row-major, ld = N). */
+/* x_devs[i] / y_devs[i]: operand and result of matrix i, row-major with
+ * leading dimension N (SpMM: 16-byte aligned).  One kernel launch (or one
+ * graph launch) for the whole batch, stream-ordered on `stream`. */
 int sable_batch_run(sable_batch *batch, const float *const *x_devs, float *const *y_devs, void *stream);
+/* Synchronises `stream`; SABLE_ERR_TIMEOUT if a bounded wait ran out. */
+int sable_batch_check(sable_batch *batch, void *stream);
+int sable_batch_get_info(const sable_batch *batch, sable_batch_info *out);
 int sable_batch_destroy(sable_batch *batch);
 
 /* Block features for the block model, one row of 6 floats per stored block

@@ -56,6 +56,11 @@ class BatchOpts(ctypes.Structure):
     _fields_ = [("ctas_per_sm", c_int32), ("use_graph", c_int32)]
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("n_mats", c_int32), ("n_ctas", c_int32), ("n_units", c_int64), ("device_bytes", c_int64),
+                ("smem_bytes", c_int32), ("stage_bytes", c_int32)]
+
+
 # name -> (restype, argtypes); every symbol of include/sable.h.
 SIGNATURES = {
     "sable_plan_create": (c_int, [POINTER(VbrcDesc), POINTER(PlanOpts), POINTER(c_void_p)]),
@@ -73,6 +78,8 @@ SIGNATURES = {
     "sable_plan_chunk_tiles": (c_int, [c_void_p, c_void_p]),
     "sable_batch_create": (c_int, [c_void_p, c_int32, c_void_p, POINTER(BatchOpts), POINTER(c_void_p)]),
     "sable_batch_run": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sable_batch_check": (c_int, [c_void_p, c_void_p]),
+    "sable_batch_get_info": (c_int, [c_void_p, POINTER(BatchInfo)]),
     "sable_batch_destroy": (c_int, [c_void_p]),
     "sable_block_features": (c_int, [POINTER(VbrcDesc), c_int32, c_void_p]),
     "sable_mlp_create": (c_int, [POINTER(c_void_p)]),

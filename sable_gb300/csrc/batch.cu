@@ -1,0 +1,516 @@
+// Batched VBR SpMV / SpMM: many matrices, one persistent kernel.
+//
+// The reference runs one generated program per matrix; serving many small
+// and mid-size matrices that way leaves the GPU idle between launches and
+// gives every launch its own tail.  A batch merges the item records of all
+// its plans into one device buffer (each record's header carries its matrix
+// index) and builds one work queue of units:
+//   SpMV unit   one item record of a width-1 matrix
+//   SpMM unit   one (item record, N-slice) pair, FP32 or split-BF16
+// sorted by class (split-BF16 SpMM, FP32 SpMM, SpMV) and within a class by
+// size, largest first.  A grid of SMs x k persistent CTAs takes units in
+// queue order from an atomic head, so the largest units start first and the
+// small ones fill the tail (greedy list scheduling).
+//
+// SpMV units run the CTA-per-item body (spmv_item.cuh) from a 2-stage TMA
+// ring: when a CTA takes SpMV unit u it also takes the next unit and, if
+// that is an SpMV unit too, starts its record's bulk copy into the other
+// stage before computing u.  SpMM units run the bodies of spmm_item.cuh
+// from global memory; no copy is in flight while one runs (their shared
+// memory overlaps the stages).  Every mbarrier wait is bounded; on expiry the
+// batch's error flag is set and the CTA waits (bounded) for its own copies
+// and leaves.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "sable.h"
+#include "plan_internal.h"
+#include "spmv_item.cuh"
+#include "spmm_item.cuh"
+
+namespace {
+
+enum UnitKind : int16_t {
+    U_SPMV = 0,
+    U_F32_16, U_F32_32, U_F32_64,
+    U_TC2_32, U_TC2_64,
+    U_TC3_32, U_TC3_64,
+};
+
+struct BatchUnit {
+    int32_t item;    // index into the merged item table
+    int16_t slice;   // N-slice (SpMM)
+    int16_t kind;
+};
+static_assert(sizeof(BatchUnit) == 8, "BatchUnit must stay 8 bytes");
+
+struct BatchArgs {
+    const unsigned char *records;
+    const ItemRef *items;
+    const BatchUnit *units;
+    const MatIO *mats;
+    int *head;           // queue head, zero before each launch
+    int *error;
+    int n_units;
+    int stage_bytes;     // bytes of one SpMV stage (>= largest SpMV record)
+};
+
+__device__ __forceinline__ void run_spmm_unit(const BatchUnit U, const unsigned char *R, const MatIO &io,
+                                              unsigned char *smem) {
+    switch (U.kind) {
+        case U_F32_16: spmm_fp32_item<16>(R, io, U.slice, io.part_stride, smem); break;
+        case U_F32_32: spmm_fp32_item<32>(R, io, U.slice, io.part_stride, smem); break;
+        case U_F32_64: spmm_fp32_item<64>(R, io, U.slice, io.part_stride, smem); break;
+        case U_TC2_32: spmm_tc_item<32, 2>(R, io, U.slice, io.part_stride, smem); break;
+        case U_TC2_64: spmm_tc_item<64, 2>(R, io, U.slice, io.part_stride, smem); break;
+        case U_TC3_32: spmm_tc_item<32, 3>(R, io, U.slice, io.part_stride, smem); break;
+        case U_TC3_64: spmm_tc_item<64, 3>(R, io, U.slice, io.part_stride, smem); break;
+        default: break;
+    }
+}
+
+__global__ void __launch_bounds__(SABLE_THREADS, 2)
+batch_kernel(const BatchArgs b) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    float *red = reinterpret_cast<float *>(smem);
+    float *ysw = red + RED_FLOATS;
+    unsigned char *stage[2] = {smem + STAGE_OFF, smem + STAGE_OFF + b.stage_bytes};
+    __shared__ __align__(8) unsigned long long s_bar[2];
+    __shared__ int s_cur, s_pref, s_next, s_next_pref, s_last;
+    const int tid = threadIdx.x;
+    const unsigned bar[2] = {smem_addr(&s_bar[0]), smem_addr(&s_bar[1])};
+    unsigned phase[2] = {0u, 0u};  // control thread: parity of each stage's next wait
+    if (tid == CTRL) {
+        mbar_init(bar[0]);
+        mbar_init(bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_cur = atomicAdd(b.head, 1);
+        s_pref = 0;
+    }
+    for (int i = tid; i < RED_FLOATS; i += SABLE_THREADS) ysw[i] = 0.f;
+    __syncthreads();
+    int st = 0;  // stage of the next SpMV unit
+    while (true) {
+        const int u = s_cur;
+        const int pref = s_pref;
+        if (u >= b.n_units) break;
+        const BatchUnit U = b.units[u];
+        if (U.kind == U_SPMV) {
+            bool bad = false, landed = true;
+            int next_in_flight = 0;
+            const ItemRef ref = b.items[U.item];
+            if (tid == CTRL) {
+                if (!pref) tma_record(bar[st], stage[st], b.records + ref.off, (unsigned)ref.bytes);
+                const int un = atomicAdd(b.head, 1);
+                if (un < b.n_units) {
+                    const BatchUnit V = b.units[un];
+                    if (V.kind == U_SPMV) {
+                        const ItemRef r2 = b.items[V.item];
+                        tma_record(bar[st ^ 1], stage[st ^ 1], b.records + r2.off, (unsigned)r2.bytes);
+                        next_in_flight = 1;
+                    }
+                }
+                s_next = un;
+                s_next_pref = next_in_flight;
+                landed = mbar_wait(bar[st], phase[st]);
+                if (landed) phase[st] ^= 1u;
+                bad = !landed || reinterpret_cast<const ItemHeader *>(stage[st])->bytes != ref.bytes;
+            }
+            if (__syncthreads_or(bad)) {
+                if (tid == CTRL) {
+                    atomicExch(b.error, 1);
+                    if (!landed) mbar_wait(bar[st], phase[st]);
+                    if (next_in_flight) mbar_wait(bar[st ^ 1], phase[st ^ 1]);
+                }
+                return;
+            }
+            const unsigned char *R = stage[st];
+            const ItemHeader hd = *reinterpret_cast<const ItemHeader *>(R);
+            const MatIO &io = b.mats[hd.mat];
+            cta_accumulate(R, hd, io.x, nullptr, red, ysw);
+            __syncthreads();
+            cta_finish(hd, io, red, ysw, &s_last);
+            st ^= 1;
+        } else {
+            if (tid == CTRL) {
+                s_next = atomicAdd(b.head, 1);
+                s_next_pref = 0;
+            }
+            const ItemRef ref = b.items[U.item];
+            const unsigned char *R = b.records + ref.off;
+            if (reinterpret_cast<const ItemHeader *>(R)->bytes == ref.bytes) {
+                const MatIO &io = b.mats[reinterpret_cast<const ItemHeader *>(R)->mat];
+                run_spmm_unit(U, R, io, smem);
+            } else if (tid == CTRL) {
+                atomicExch(b.error, 1);
+            }
+            __syncthreads();
+            // the SpMM body used the whole shared memory: restore the zero CSR rows
+            for (int i = tid; i < RED_FLOATS; i += SABLE_THREADS) ysw[i] = 0.f;
+        }
+        __syncthreads();
+        if (tid == CTRL) {
+            s_cur = s_next;
+            s_pref = s_next_pref;
+        }
+        __syncthreads();
+    }
+}
+
+// Writes each merged record's matrix index into its header.
+__global__ void patch_mat_kernel(unsigned char *records, const ItemRef *items, const int32_t *mat, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) reinterpret_cast<ItemHeader *>(records + items[k].off)->mat = mat[k];
+}
+
+int spmm_nt(int N) { return N <= 16 ? 16 : N <= 32 ? 32 : 64; }
+
+int16_t spmm_kind(int nt, int tc_terms) {
+    if (tc_terms == 0) return nt == 16 ? U_F32_16 : nt == 32 ? U_F32_32 : U_F32_64;
+    if (tc_terms == 2) return nt == 32 ? U_TC2_32 : U_TC2_64;
+    return nt == 32 ? U_TC3_32 : U_TC3_64;
+}
+
+int spmm_unit_smem(int16_t kind) {
+    switch (kind) {
+        case U_F32_16: return SpmmSmem<16>::TOTAL;
+        case U_F32_32: return SpmmSmem<32>::TOTAL;
+        case U_F32_64: return SpmmSmem<64>::TOTAL;
+        case U_TC2_32: case U_TC3_32: return TcSmem<32>::TOTAL;
+        case U_TC2_64: case U_TC3_64: return TcSmem<64>::TOTAL;
+        default: return 0;
+    }
+}
+
+}  // namespace
+
+struct sable_batch {
+    int device = 0;
+    int n_mats = 0;
+    std::vector<int32_t> width;
+    std::vector<int64_t> n_rows, n_cols;
+    unsigned char *d_records = nullptr;
+    ItemRef *d_items = nullptr;
+    BatchUnit *d_units = nullptr;
+    MatIO *d_mats = nullptr;
+    MatIO *h_mats = nullptr;          // pinned staging of the matrix table
+    float *d_partial = nullptr;
+    int *d_counters = nullptr;
+    int *d_head = nullptr;
+    int *d_error = nullptr;
+    int64_t n_units = 0, device_bytes = 0;
+    int stage_bytes = 0, smem = 0, n_ctas = 0;
+    bool mats_valid = false;
+    bool use_graph = false;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+using namespace sable;
+
+namespace {
+
+int batch_launch(sable_batch *bt, cudaStream_t s) {
+    BatchArgs a;
+    a.records = bt->d_records;
+    a.items = bt->d_items;
+    a.units = bt->d_units;
+    a.mats = bt->d_mats;
+    a.head = bt->d_head;
+    a.error = bt->d_error;
+    a.n_units = (int)bt->n_units;
+    a.stage_bytes = bt->stage_bytes;
+    cudaError_t e = cudaMemsetAsync(bt->d_head, 0, sizeof(int), s);
+    if (e != cudaSuccess) return cuda_fail(e, "batch queue reset");
+    batch_kernel<<<bt->n_ctas, SABLE_THREADS, bt->smem, s>>>(a);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "batch kernel launch");
+    return SABLE_OK;
+}
+
+template <class T>
+int dev_alloc(T **p, size_t n, int64_t *bytes, const char *what) {
+    cudaError_t e = cudaMalloc((void **)p, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) return fail(SABLE_ERR_NOMEM, "batch %s: %s", what, cudaGetErrorString(e));
+    *bytes += (int64_t)(std::max<size_t>(n, 1) * sizeof(T));
+    return SABLE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sable_batch_destroy(sable_batch *bt) {
+    if (!bt) return SABLE_OK;
+    int prev = -1;
+    cudaGetDevice(&prev);
+    cudaSetDevice(bt->device);
+    if (bt->done) cudaEventSynchronize(bt->done);
+    if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    if (bt->cap_stream) cudaStreamDestroy(bt->cap_stream);
+    if (bt->done) cudaEventDestroy(bt->done);
+    cudaFree(bt->d_records);
+    cudaFree(bt->d_items);
+    cudaFree(bt->d_units);
+    cudaFree(bt->d_mats);
+    cudaFree(bt->d_partial);
+    cudaFree(bt->d_counters);
+    cudaFree(bt->d_head);
+    cudaFree(bt->d_error);
+    if (bt->h_mats) cudaFreeHost(bt->h_mats);
+    if (prev >= 0) cudaSetDevice(prev);
+    delete bt;
+    return SABLE_OK;
+}
+
+int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t *widths,
+                       const sable_batch_opts *opts, sable_batch **out) {
+    if (!plans || !widths || !out || n_plans <= 0) return fail(SABLE_ERR_ARG, "bad argument");
+    *out = nullptr;
+    sable_batch_opts o{};
+    if (opts) o = *opts;
+    if (o.ctas_per_sm < 0) return fail(SABLE_ERR_ARG, "ctas_per_sm must be >= 0");
+    for (int i = 0; i < n_plans; ++i) {
+        if (!plans[i]) return fail(SABLE_ERR_ARG, "plan %d is null", i);
+        if (plans[i]->device != plans[0]->device) return fail(SABLE_ERR_ARG, "plans on different devices");
+        if (widths[i] < 1 || (widths[i] > 1 && (widths[i] & 3)))
+            return fail(SABLE_ERR_UNSUPPORTED, "width %d of matrix %d: 1, or a multiple of 4", widths[i], i);
+    }
+    int rc = set_device(plans[0]->device);
+    if (rc) return rc;
+    sable_batch *bt = new (std::nothrow) sable_batch();
+    if (!bt) return fail(SABLE_ERR_NOMEM, "host allocation");
+    bt->device = plans[0]->device;
+    bt->n_mats = n_plans;
+    bt->use_graph = o.use_graph != 0;
+    auto bail = [&](int code) {
+        sable_batch_destroy(bt);
+        return code;
+    };
+
+    // merged records and item table; per-matrix scratch and the unit queue
+    int64_t rec_total = 0, n_items = 0;
+    for (int i = 0; i < n_plans; ++i) {
+        rec_total += plans[i]->records_bytes;
+        n_items += plans[i]->n_items;
+    }
+    if (n_items >= INT32_MAX) return bail(fail(SABLE_ERR_UNSUPPORTED, "batch of %lld items", (long long)n_items));
+    std::vector<ItemRef> items;
+    std::vector<int32_t> item_mat;
+    items.reserve(n_items);
+    item_mat.reserve(n_items);
+    std::vector<MatIO> mats(n_plans);
+    struct Sortable {
+        int32_t cls;
+        int64_t cost;
+        BatchUnit u;
+    };
+    std::vector<Sortable> q;
+    int64_t partial_total = 0, counter_total = 0, rec_base = 0;
+    std::vector<int64_t> part_off(n_plans), cnt_off(n_plans);
+    for (int i = 0; i < n_plans; ++i) {
+        const sable_plan *p = plans[i];
+        const int W = widths[i];
+        bt->width.push_back(W);
+        bt->n_rows.push_back(p->n_rows);
+        bt->n_cols.push_back(p->n_cols);
+        const int nt = W == 1 ? 1 : spmm_nt(W);
+        const int slices = W == 1 ? 1 : (W + nt - 1) / nt;
+        const int terms = (W >= 32 && p->spmm_tc) ? (p->spmm_tc == SABLE_TC_SPLIT3 ? 3 : 2) : 0;
+        const int16_t kind = W == 1 ? (int16_t)U_SPMV : spmm_kind(nt, terms);
+        const int32_t cls = W == 1 ? 2 : (terms ? 0 : 1);
+        const int64_t nsplit = std::max<int32_t>(p->n_split_tiles, 1);
+        MatIO &m = mats[i];
+        memset(&m, 0, sizeof m);
+        m.ldx = m.ldy = W;
+        m.N = W;
+        m.pad = (int32_t)nsplit;
+        m.part_stride = p->n_partial * nt;
+        // regions start on 256-byte boundaries: the SpMM bodies move float4s
+        part_off[i] = partial_total;
+        cnt_off[i] = counter_total;
+        partial_total += (std::max<int64_t>(p->n_partial * nt * slices, 1) + 63) & ~(int64_t)63;
+        counter_total += nsplit * slices;
+        for (int64_t k = 0; k < p->n_items; ++k) {
+            ItemRef r = p->items_host[k];
+            r.off += rec_base;
+            const int32_t idx = (int32_t)items.size();
+            items.push_back(r);
+            item_mat.push_back(i);
+            if (kind == U_SPMV) bt->stage_bytes = std::max(bt->stage_bytes, r.bytes);
+            for (int sl = 0; sl < slices; ++sl) {
+                Sortable s;
+                s.cls = cls;
+                s.cost = (int64_t)r.bytes * (W == 1 ? 1 : nt);
+                s.u.item = idx;
+                s.u.slice = (int16_t)sl;
+                s.u.kind = kind;
+                q.push_back(s);
+            }
+        }
+        rec_base += p->records_bytes;
+    }
+    std::stable_sort(q.begin(), q.end(), [](const Sortable &a, const Sortable &b) {
+        return a.cls != b.cls ? a.cls < b.cls : a.cost > b.cost;
+    });
+    std::vector<BatchUnit> units(q.size());
+    int spmm_smem = 0;
+    for (size_t k = 0; k < q.size(); ++k) {
+        units[k] = q[k].u;
+        spmm_smem = std::max(spmm_smem, spmm_unit_smem(q[k].u.kind));
+    }
+    bt->n_units = (int64_t)units.size();
+    if (bt->n_units >= INT32_MAX) return bail(fail(SABLE_ERR_UNSUPPORTED, "batch of %lld units", (long long)bt->n_units));
+    bt->stage_bytes = (bt->stage_bytes + 127) & ~127;
+    bt->smem = std::max(bt->stage_bytes ? STAGE_OFF + 2 * bt->stage_bytes : 0, spmm_smem);
+    bt->smem = std::max(bt->smem, STAGE_OFF);
+
+    int64_t &bytes = bt->device_bytes;
+    if ((rc = dev_alloc(&bt->d_records, (size_t)rec_total, &bytes, "records"))) return bail(rc);
+    if ((rc = dev_alloc(&bt->d_items, items.size(), &bytes, "items"))) return bail(rc);
+    if ((rc = dev_alloc(&bt->d_units, units.size(), &bytes, "units"))) return bail(rc);
+    if ((rc = dev_alloc(&bt->d_mats, mats.size(), &bytes, "matrix table"))) return bail(rc);
+    if ((rc = dev_alloc(&bt->d_partial, (size_t)partial_total, &bytes, "partials"))) return bail(rc);
+    if ((rc = dev_alloc(&bt->d_counters, (size_t)counter_total, &bytes, "counters"))) return bail(rc);
+    if ((rc = dev_alloc(&bt->d_head, 1, &bytes, "queue head"))) return bail(rc);
+    if ((rc = dev_alloc(&bt->d_error, 1, &bytes, "error flag"))) return bail(rc);
+    int32_t *d_item_mat = nullptr;
+    int64_t scratch_bytes = 0;
+    if ((rc = dev_alloc(&d_item_mat, item_mat.size(), &scratch_bytes, "item matrices"))) return bail(rc);
+    cudaError_t e = cudaSuccess;
+    rec_base = 0;
+    for (int i = 0; i < n_plans && e == cudaSuccess; ++i) {
+        if (plans[i]->records_bytes)
+            e = cudaMemcpy(bt->d_records + rec_base, plans[i]->d_records, (size_t)plans[i]->records_bytes,
+                           cudaMemcpyDeviceToDevice);
+        rec_base += plans[i]->records_bytes;
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(bt->d_items, items.data(), items.size() * sizeof(ItemRef), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(bt->d_units, units.data(), units.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(d_item_mat, item_mat.data(), item_mat.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !items.empty()) {
+        patch_mat_kernel<<<(unsigned)((items.size() + 255) / 256), 256>>>(bt->d_records, bt->d_items, d_item_mat,
+                                                                          (int)items.size());
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    cudaFree(d_item_mat);
+    if (e == cudaSuccess) e = cudaMemset(bt->d_counters, 0, (size_t)std::max<int64_t>(counter_total, 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(bt->d_error, 0, sizeof(int));
+    if (e != cudaSuccess) return bail(cuda_fail(e, "batch upload"));
+    for (int i = 0; i < n_plans; ++i) {
+        mats[i].partial = bt->d_partial + part_off[i];
+        mats[i].counters = bt->d_counters + cnt_off[i];
+    }
+    e = cudaMallocHost((void **)&bt->h_mats, mats.size() * sizeof(MatIO));
+    if (e != cudaSuccess) return bail(cuda_fail(e, "batch pinned table"));
+    memcpy(bt->h_mats, mats.data(), mats.size() * sizeof(MatIO));
+
+    // launch shape
+    int dev_max = 0, sms = 0, occ = 0;
+    cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, bt->device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, bt->device);
+    if (bt->smem > dev_max)
+        return bail(fail(SABLE_ERR_UNSUPPORTED, "batch needs %d bytes of shared memory per CTA (device: %d)", bt->smem,
+                         dev_max));
+    e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bt->smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, SABLE_THREADS, bt->smem);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "batch kernel occupancy"));
+    occ = std::max(occ, 1);
+    const int per_sm = o.ctas_per_sm ? std::min(o.ctas_per_sm, occ) : occ;
+    bt->n_ctas = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, std::max<int64_t>(bt->n_units, 1)));
+    e = cudaEventCreateWithFlags(&bt->done, cudaEventDisableTiming);
+    if (e != cudaSuccess) return bail(cuda_fail(e, "batch event"));
+    if (bt->use_graph) {
+        e = cudaStreamCreateWithFlags(&bt->cap_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return bail(cuda_fail(e, "batch capture stream"));
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(bt->cap_stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return bail(cuda_fail(e, "batch graph capture"));
+        rc = batch_launch(bt, bt->cap_stream);
+        e = cudaStreamEndCapture(bt->cap_stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return bail(rc);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&bt->exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) return bail(cuda_fail(e, "batch graph instantiate"));
+    }
+    *out = bt;
+    return SABLE_OK;
+}
+
+int sable_batch_run(sable_batch *bt, const float *const *x_devs, float *const *y_devs, void *stream) {
+    if (!bt || !x_devs || !y_devs) return fail(SABLE_ERR_ARG, "null argument");
+    int rc = set_device(bt->device);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    bool changed = !bt->mats_valid;
+    for (int i = 0; i < bt->n_mats; ++i) {
+        if (!x_devs[i] || !y_devs[i]) return fail(SABLE_ERR_ARG, "null operand of matrix %d", i);
+        if (bt->width[i] > 1 && (((uintptr_t)x_devs[i] & 15) || ((uintptr_t)y_devs[i] & 15)))
+            return fail(SABLE_ERR_UNSUPPORTED, "SpMM operands of matrix %d must be 16-byte aligned", i);
+        changed |= bt->h_mats[i].x != x_devs[i] || bt->h_mats[i].y != y_devs[i];
+    }
+    cudaError_t e;
+    if (changed) {
+        // the previous run's copy of the pinned table must have completed
+        e = cudaEventSynchronize(bt->done);
+        if (e != cudaSuccess) return cuda_fail(e, "batch table wait");
+        for (int i = 0; i < bt->n_mats; ++i) {
+            bt->h_mats[i].x = x_devs[i];
+            bt->h_mats[i].y = y_devs[i];
+        }
+        e = cudaMemcpyAsync(bt->d_mats, bt->h_mats, (size_t)bt->n_mats * sizeof(MatIO), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return cuda_fail(e, "batch table upload");
+        bt->mats_valid = true;
+    }
+    if (bt->exec) {
+        e = cudaGraphLaunch(bt->exec, s);
+        if (e != cudaSuccess) return cuda_fail(e, "batch graph launch");
+    } else if ((rc = batch_launch(bt, s))) {
+        return rc;
+    }
+    e = cudaEventRecord(bt->done, s);
+    if (e != cudaSuccess) return cuda_fail(e, "batch event record");
+    return SABLE_OK;
+}
+
+int sable_batch_check(sable_batch *bt, void *stream) {
+    if (!bt) return fail(SABLE_ERR_ARG, "null batch");
+    int rc = set_device(bt->device);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int flag = 0;
+    cudaError_t e = cudaMemcpyAsync(&flag, bt->d_error, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "batch check");
+    if (flag) {
+        cudaMemsetAsync(bt->d_error, 0, sizeof(int), s);
+        cudaStreamSynchronize(s);
+        return fail(SABLE_ERR_TIMEOUT, "a bounded device wait ran out (or a record failed its check) in the batch");
+    }
+    return SABLE_OK;
+}
+
+int sable_batch_get_info(const sable_batch *bt, sable_batch_info *out) {
+    if (!bt || !out) return fail(SABLE_ERR_ARG, "null argument");
+    out->n_mats = bt->n_mats;
+    out->n_ctas = bt->n_ctas;
+    out->n_units = bt->n_units;
+    out->device_bytes = bt->device_bytes;
+    out->smem_bytes = bt->smem;
+    out->stage_bytes = bt->stage_bytes;
+    return SABLE_OK;
+}
+
+}  // extern "C"

@@ -37,6 +37,7 @@ int plan_upload(sable_plan *p, const Layout &L) {
     p->n_split_tiles = L.n_split_tiles;
     p->max_item_bytes = std::max(L.max_item_bytes, 64);
     p->max_xg_floats = std::max(L.max_xg_floats, 4);
+    p->records_bytes = (int64_t)L.records.size();
     int64_t bytes = 0;
     int rc;
     // item table, largest first (one CTA per item launches and the timed form)

@@ -39,6 +39,7 @@ struct sable_plan {
     int32_t n_rows = 0, n_cols = 0;
     int row_tile = 0, item_bytes = 0, spmm_tc = 0, schedule = 0;
     unsigned char *d_records = nullptr;
+    int64_t records_bytes = 0;
     ItemRef *d_items = nullptr;          // item table, largest first
     WorkRef *d_work = nullptr;           // warp-worker lists (persistent schedule)
     int *d_cta_begin = nullptr;          // worker ranges into d_work

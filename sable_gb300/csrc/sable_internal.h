@@ -89,7 +89,8 @@ struct MatIO {
     int *pcounters;     // multi-part tile arrival counters (self-resetting)
     int64_t ldx, ldy;
     int32_t N;          // 1 for SpMV
-    int32_t pad;
+    int32_t pad;        // SpMM: split-tile counters per N-slice
+    int64_t part_stride;  // SpMM: partial floats per N-slice (batch kernel)
 };
 
 struct LaunchArgs {

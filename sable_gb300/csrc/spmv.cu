@@ -29,223 +29,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "sable_internal.h"
+#include "spmv_item.cuh"
 
 namespace {
-
-constexpr unsigned FULL = 0xffffffffu;
-constexpr int NWARP = SABLE_NWARP;
-constexpr int RED_FLOATS = NWARP * SABLE_MAX_ROW_TILE;    // dense partials (CTA kernel)
-constexpr int STAGE_OFF = 2 * RED_FLOATS * 4;             // + CSR partials, bytes
-constexpr unsigned long long WAIT_NS = 2000000000ull;
-constexpr int CTRL = SABLE_THREADS - 1;                    // control thread (CTA kernel)
-constexpr int WCTRL = 31;                                  // control lane (warp kernel)
-constexpr int ROWBUF_FLOATS = SABLE_MAX_ROW_TILE + 32;     // warp kernel: CSR row sums + dense temp
-
-__device__ __forceinline__ unsigned smem_addr(const void *p) {
-    return static_cast<unsigned>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void mbar_init(unsigned bar) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
-}
-
-// Wait for phase `parity` of an mbarrier, giving up after WAIT_NS.
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-    unsigned done = 0;
-    const unsigned long long t0 = global_ns();
-    while (true) {
-        asm volatile(
-            "{\n .reg .pred p;\n"
-            " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
-            " selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done) : "r"(bar), "r"(parity), "r"(1000000u) : "memory");
-        if (done) return true;
-        if (global_ns() - t0 > WAIT_NS) return false;
-    }
-}
-
-// Release-acquire arrival on a split-tile counter (one thread, after the
-// partial-sum stores of its CTA / warp are ordered before it).
-__device__ __forceinline__ int arrive_acq_rel(int *cnt) {
-    int old;
-    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(cnt) : "memory");
-    return old;
-}
-
-// One thread: expect `bytes` on `bar` and copy the record into `dst`.
-__device__ __forceinline__ void tma_record(unsigned bar, void *dst, const unsigned char *src, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(bar), "r"(bytes) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 :: "r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(bar) : "memory");
-}
-
-__device__ __forceinline__ void cp_async4(void *dst, const float *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" :: "r"(smem_addr(dst)), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" :: "n"(N) : "memory"); }
-
-__device__ __forceinline__ float dot4(const float4 a, const float4 b, float acc) {
-    acc = fmaf(a.x, b.x, acc);
-    acc = fmaf(a.y, b.y, acc);
-    acc = fmaf(a.z, b.z, acc);
-    acc = fmaf(a.w, b.w, acc);
-    return acc;
-}
-
-__device__ __forceinline__ float4 xquad(const int4 *xc, int q, const float *__restrict__ x) {
-    const int4 c = xc[q];
-    return make_float4(__ldg(x + c.x), __ldg(x + c.y), __ldg(x + c.z), __ldg(x + c.w));
-}
-
-__device__ __forceinline__ const MatIO &mat_of(const LaunchArgs &a, int mat) { return a.mats ? a.mats[mat] : a.mat0; }
-
-// ---------------------------------------------------------------------------
-// CSR rows of one item with groups of g lanes per row: adds each row's sum
-// into rowsum[row] (one writer per row).  Rows [r_lo, h), entries clipped
-// to [e_lo, e_hi).  xv(i, col) gives the x value of entry i.
-// ---------------------------------------------------------------------------
-template <class XV>
-__device__ __forceinline__ void csr_rows(const int *rp, const uint2 *E, int h, int g, int e_lo, int e_hi, int lane,
-                                         float *rowsum, XV xv) {
-    if (e_lo >= e_hi) return;
-    const int gpw = 32 / g, sg = lane / g, sl = lane % g;
-    int lo = 0, hi = h - 1;  // first row with entries at or after e_lo
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (rp[mid + 1] > e_lo) hi = mid; else lo = mid + 1;
-    }
-    for (int r0 = lo; r0 < h && rp[r0] < e_hi; r0 += gpw) {
-        const int r = r0 + sg;
-        int b = e_hi, e = e_hi;
-        if (r < h) {
-            b = max(rp[r], e_lo);
-            e = min(rp[r + 1], e_hi);
-        }
-        const int nsteps = __reduce_max_sync(FULL, e > b ? (e - b + 2 * g - 1) / (2 * g) : 0);
-        float s = 0.f;
-        for (int k = 0; k < nsteps; ++k) {
-            const int i0 = b + 2 * k * g + sl, i1 = i0 + g;
-            if (i0 < e) {
-                const uint2 u = E[i0];
-                s = fmaf(__uint_as_float(u.x), xv(i0, u.y), s);
-            }
-            if (i1 < e) {
-                const uint2 u = E[i1];
-                s = fmaf(__uint_as_float(u.x), xv(i1, u.y), s);
-            }
-        }
-        for (int o = g >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
-        if (sl == 0 && r < h && e > b) rowsum[r] += s;
-    }
-}
-
-// ---------------------------------------------------------------------------
-// CTA-per-item kernel
-// ---------------------------------------------------------------------------
-// x values of an item come either from x through L1 (XG == nullptr) or from
-// the item's gathered copy in shared memory: xg[0, 4nq) for the panel
-// columns, xg[4nq, 4nq + ns) for the CSR entries.
-__device__ __forceinline__ void cta_accumulate(const unsigned char *R, const ItemHeader &hd, const float *__restrict__ x,
-                                               const float *xg, float *red, float *ysw) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int h = hd.h, nq = hd.nq, ns = hd.ns;
-    const int4 *xc = reinterpret_cast<const int4 *>(R + hd.xcol_off);
-    const float4 *P = reinterpret_cast<const float4 *>(R + hd.panel_off);
-    const float4 *xg4 = reinterpret_cast<const float4 *>(xg);
-    auto xq = [&](int q) { return xg ? xg4[q] : xquad(xc, q, x); };
-    if (h <= 32) {
-        const int qpw = 32 / h;
-        const bool act = lane < qpw * h;
-        const int r = lane % h, s = lane / h;
-        float acc = 0.f, accb = 0.f;
-        if (nq > 0 && act) {
-            const int step = NWARP * qpw;
-            int q = warp * qpw + s;
-            for (; q + step < nq; q += 2 * step) {
-                const float4 x0 = xq(q), x1 = xq(q + step);
-                acc = dot4(P[q * h + r], x0, acc);
-                accb = dot4(P[(q + step) * h + r], x1, accb);
-            }
-            if (q < nq) acc = dot4(P[q * h + r], xq(q), acc);
-        }
-        red[warp * SABLE_MAX_ROW_TILE + lane] = act ? acc + accb : 0.f;
-    } else {
-        float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
-        const bool v1 = lane + 32 < h, v2 = lane + 64 < h, v3 = lane + 96 < h;
-        for (int q = warp; q < nq; q += NWARP) {
-            const float4 xa = xq(q);
-            const float4 *Pa = P + q * h + lane;
-            acc0 = dot4(Pa[0], xa, acc0);
-            if (v1) acc1 = dot4(Pa[32], xa, acc1);
-            if (v2) acc2 = dot4(Pa[64], xa, acc2);
-            if (v3) acc3 = dot4(Pa[96], xa, acc3);
-        }
-        float *rw = red + warp * SABLE_MAX_ROW_TILE;
-        rw[lane] = acc0;
-        if (v1) rw[lane + 32] = acc1;
-        if (v2) rw[lane + 64] = acc2;
-        if (v3) rw[lane + 96] = acc3;
-    }
-    if (ns > 0) {
-        const int *rp = reinterpret_cast<const int *>(R + hd.rp_off);
-        const uint2 *E = reinterpret_cast<const uint2 *>(R + hd.csr_off);
-        const int e_lo = (int)(((int64_t)ns * warp) / NWARP), e_hi = (int)(((int64_t)ns * (warp + 1)) / NWARP);
-        const float *xe = xg ? xg + 4 * nq : nullptr;
-        csr_rows(rp, E, h, hd.g, e_lo, e_hi, lane, ysw + warp * SABLE_MAX_ROW_TILE,
-                 [&](int i, unsigned col) { return xe ? xe[i] : __ldg(x + col); });
-    }
-}
-
-// Row sums in a fixed order, output, split-tile reduction; leaves ysw zero.
-__device__ __forceinline__ void cta_finish(const ItemHeader &hd, const MatIO &io, float *red, float *ysw, int *s_last) {
-    const int tid = threadIdx.x;
-    const int h = hd.h;
-    const bool split = hd.nitem > 1;
-    if (tid < h) {
-        const int i = tid;
-        float sd = 0.f;
-        if (h <= 32) {
-            const int qpw = 32 / h;
-#pragma unroll
-            for (int w = 0; w < NWARP; ++w)
-                for (int s2 = 0; s2 < qpw; ++s2) sd += red[w * SABLE_MAX_ROW_TILE + s2 * h + i];
-        } else {
-#pragma unroll
-            for (int w = 0; w < NWARP; ++w) sd += red[w * SABLE_MAX_ROW_TILE + i];
-        }
-        float sp = 0.f;
-#pragma unroll
-        for (int w = 0; w < NWARP; ++w) {
-            sp += ysw[w * SABLE_MAX_ROW_TILE + i];
-            ysw[w * SABLE_MAX_ROW_TILE + i] = 0.f;
-        }
-        const float tot = sd + sp;
-        if (!split) io.y[hd.row0 + i] = tot;
-        else io.partial[hd.part_base + (int64_t)hd.kidx * h + i] = tot;
-    }
-    if (split) {
-        if (tid < h) __threadfence();  // this CTA's partial sums, visible at device scope
-        __syncthreads();
-        if (tid == CTRL) *s_last = (arrive_acq_rel(io.counters + hd.tile) == hd.nitem - 1);
-        __syncthreads();
-        if (*s_last) {
-            for (int i = tid; i < h; i += SABLE_THREADS) {
-                float s = 0.f;
-                for (int k = 0; k < hd.nitem; ++k) s += __ldcg(io.partial + hd.part_base + (int64_t)k * h + i);
-                io.y[hd.row0 + i] = s;
-            }
-            if (tid == CTRL) io.counters[hd.tile] = 0;  // ready for the next launch
-        }
-    }
-}
 
 template <bool TIMED>
 __global__ void __launch_bounds__(SABLE_THREADS)

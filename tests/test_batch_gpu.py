@@ -1,0 +1,134 @@
+"""Batched SpMV / SpMM (one persistent kernel for many matrices) against the
+FP64 oracle, against the per-matrix entry points, with and without a CUDA
+graph, and the batch's argument checks."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from sable_gb300 import _lib, convert, synth
+from sable_gb300.batch import Batch
+from sable_gb300.plan import Plan
+
+pytestmark = pytest.mark.gpu
+
+
+def random_vbr(seed, n, lo=4, hi=128, p=0.05):
+    rng = np.random.default_rng(seed)
+    rs = synth.sizes_until(rng, lo, hi, n)
+    cs = synth.sizes_until(rng, lo, hi, n)
+    present = rng.random((len(rs), len(cs))) < p
+    present[0, 0] = True
+
+    def fill(rng, h, w, a, b):
+        v = rng.uniform(-1, 1, (h, w)).astype(np.float32)
+        return v if rng.random() < 0.5 else v * synth.block_pattern(rng, h, w, rng.uniform(0.02, 0.4), "uniform")
+
+    return synth.assemble(rng, rs, cs, present, fill)
+
+
+def make(seed, n, width, tc=False, chunk_bytes=0):
+    m = random_vbr(seed, n)
+    dense = np.random.default_rng(seed + 1).random(m.n_blocks) < 0.6
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense)
+    return m, comp, Plan(comp, spmm_tc=tc, chunk_bytes=chunk_bytes)
+
+
+CASES = [  # (n, width, tc, chunk_bytes)
+    (300, 1, False, 0), (2000, 1, False, 4096), (1500, 64, False, 0), (900, 64, "split3", 4096),
+    (700, 32, "split2", 0), (1200, 8, False, 0), (500, 128, "split3", 0), (4000, 1, False, 0),
+    (64, 4, False, 0), (2500, 96, False, 8192), (800, 16, False, 0), (3000, 1, False, 16384),
+]
+
+
+def build_batch(use_graph, seed0=10):
+    import torch
+    mats, plans, xs = [], [], []
+    for k, (n, w, tc, cb) in enumerate(CASES):
+        m, comp, p = make(seed0 + k, n, w, tc, cb)
+        mats.append((m, comp))
+        plans.append(p)
+        rng = np.random.default_rng(100 + k)
+        x = rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)
+        xs.append(torch.as_tensor(x).cuda())
+    b = Batch(plans, [c[1] for c in CASES], use_graph=use_graph)
+    return b, mats, plans, xs
+
+
+def check_outputs(mats, xs, ys):
+    for k, ((m, comp), x, y) in enumerate(zip(mats, xs, ys)):
+        w, tc = CASES[k][1], CASES[k][2]
+        xn = x.cpu().numpy()
+        if w == 1:
+            yr, ya = oracle.spmv_vbrc(comp, xn)
+        else:
+            yr, ya = oracle.spmm_vbr(m, xn)
+        tol = oracle.TOL_SPLIT2 if tc == "split2" else oracle.TOL
+        r = oracle.report(y.cpu().numpy(), yr, ya, tol)
+        assert r["pass"], (k, CASES[k], r)
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_matches_oracle(cuda, use_graph):
+    b, mats, plans, xs = build_batch(use_graph)
+    ys = b.outputs()
+    b.run(xs, ys)
+    b.check()
+    check_outputs(mats, xs, ys)
+    info = b.info()
+    assert info["n_mats"] == len(CASES) and info["n_units"] >= sum(p.stats()["n_chunks"] for p in plans)
+
+
+def test_batch_spmv_bitwise_equals_single_plan(cuda):
+    """SpMV units run the per-item body: identical bits to sable_spmv."""
+    import torch
+    b, mats, plans, xs = build_batch(True)
+    ys = b.outputs()
+    b.run(xs, ys)
+    torch.cuda.synchronize()
+    for k, (p, x, y) in enumerate(zip(plans, xs, ys)):
+        if CASES[k][1] == 1:
+            assert torch.equal(p.spmv(x), y), k
+
+
+def test_batch_repeat_and_new_pointers(cuda):
+    import torch
+    b, mats, plans, xs = build_batch(True, seed0=40)
+    for p in plans:
+        p.close()  # the batch keeps its own copy of the records
+    ys1 = b.outputs()
+    b.run(xs, ys1)
+    ys2 = b.outputs()
+    b.run(xs, ys2)          # new result pointers: the table is re-uploaded
+    b.run(xs, ys2)          # and replayed as is
+    xs3 = [x.clone() * 2 for x in xs]
+    ys3 = b.outputs()
+    b.run(xs3, ys3)
+    b.check()
+    torch.cuda.synchronize()
+    for a, c, d in zip(ys1, ys2, ys3):
+        assert torch.equal(a, c)
+        assert torch.equal(a * 2, d)
+
+
+def test_batch_one_ctas_per_sm(cuda):
+    b, mats, plans, xs = build_batch(False, seed0=70)
+    b2 = Batch(plans, [c[1] for c in CASES], ctas_per_sm=1, use_graph=False)
+    ys = b2.outputs()
+    b2.run(xs, ys)
+    b2.check()
+    check_outputs(mats, xs, ys)
+    import torch
+    assert b2.info()["n_ctas"] <= torch.cuda.get_device_properties(0).multi_processor_count
+
+
+def test_batch_argument_checks(cuda):
+    m, comp, p = make(5, 200, 1)
+    with pytest.raises(_lib.SableError) as e:
+        Batch([p], [6])
+    assert e.value.code == -4
+    with pytest.raises(ValueError):
+        Batch([p], [1, 4])
+    b = Batch([p], [1])
+    import torch
+    with pytest.raises(ValueError):
+        b.run([torch.zeros(3, device="cuda")], [torch.zeros(m.n_rows, device="cuda")])
