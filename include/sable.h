@@ -166,14 +166,16 @@ int sable_plan_chunk_tiles(const sable_plan *plan, int64_t *tile_of_chunk);
  * created with spmm_tc and N >= 32.  Work units are (item, N-slice) pairs of
  * every plan, sorted by class (split-BF16 SpMM, FP32 SpMM, SpMV) and, within
  * a class, by size, largest first; persistent CTAs take units in that order
- * from an atomic queue head, and every SpMV record is prefetched by TMA while
- * the previous unit is computed.  The batch copies the plans' records; the
+ * from an atomic queue head and keep several SpMV records in flight (TMA
+ * ring of `stages` records per CTA).  The batch copies the plans' records; the
  * plans may be destroyed after sable_batch_create.
  */
 typedef struct sable_batch_opts {
     int32_t ctas_per_sm;  /* persistent CTAs per SM (0: as many as fit)       */
     int32_t use_graph;    /* 1: sable_batch_run replays a CUDA graph of the
                              queue reset and the kernel launch                 */
+    int32_t stages;       /* SpMV records in flight per CTA: 2, 3, 4, 6 or 8
+                             (SpMV-only batches), 2 or 4 with SpMM (0: auto)   */
 } sable_batch_opts;
 
 typedef struct sable_batch_info {
@@ -183,6 +185,7 @@ typedef struct sable_batch_info {
     int64_t device_bytes;     /* records, tables and scratch of the batch    */
     int32_t smem_bytes;       /* dynamic shared memory per CTA               */
     int32_t stage_bytes;      /* TMA staging bytes per SpMV stage            */
+    int32_t stages;           /* SpMV ring depth                              */
 } sable_batch_info;
 
 int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t *widths,

@@ -53,12 +53,12 @@ class PlanStats(ctypes.Structure):
 
 
 class BatchOpts(ctypes.Structure):
-    _fields_ = [("ctas_per_sm", c_int32), ("use_graph", c_int32)]
+    _fields_ = [("ctas_per_sm", c_int32), ("use_graph", c_int32), ("stages", c_int32)]
 
 
 class BatchInfo(ctypes.Structure):
     _fields_ = [("n_mats", c_int32), ("n_ctas", c_int32), ("n_units", c_int64), ("device_bytes", c_int64),
-                ("smem_bytes", c_int32), ("stage_bytes", c_int32)]
+                ("smem_bytes", c_int32), ("stage_bytes", c_int32), ("stages", c_int32)]
 
 
 # name -> (restype, argtypes); every symbol of include/sable.h.

@@ -19,7 +19,7 @@ from .plan import Plan, _stream_handle
 
 
 class Batch:
-    def __init__(self, plans: list[Plan], widths, ctas_per_sm: int = 0, use_graph: bool = True):
+    def __init__(self, plans: list[Plan], widths, ctas_per_sm: int = 0, use_graph: bool = True, stages: int = 0):
         widths = np.ascontiguousarray(widths, dtype=np.int32)
         if len(widths) != len(plans) or not len(plans):
             raise ValueError("one width per plan, at least one plan")
@@ -27,7 +27,7 @@ class Batch:
         self.n_rows = [p.n_rows for p in plans]
         self.n_cols = [p.n_cols for p in plans]
         handles = (ctypes.c_void_p * len(plans))(*[p.handle for p in plans])
-        opts = _lib.BatchOpts(int(ctas_per_sm), int(bool(use_graph)))
+        opts = _lib.BatchOpts(int(ctas_per_sm), int(bool(use_graph)), int(stages))
         h = ctypes.c_void_p()
         _lib.check(_lib.load().sable_batch_create(handles, len(plans), widths.ctypes.data, ctypes.byref(opts),
                                                   ctypes.byref(h)), "sable_batch_create")

@@ -12,14 +12,15 @@
 // queue order from an atomic head, so the largest units start first and the
 // small ones fill the tail (greedy list scheduling).
 //
-// SpMV units run the CTA-per-item body (spmv_item.cuh) from a 2-stage TMA
-// ring: when a CTA takes SpMV unit u it also takes the next unit and, if
-// that is an SpMV unit too, starts its record's bulk copy into the other
-// stage before computing u.  SpMM units run the bodies of spmm_item.cuh
-// from global memory; no copy is in flight while one runs (their shared
-// memory overlaps the stages).  Every mbarrier wait is bounded; on expiry the
+// SpMM units run the bodies of spmm_item.cuh from global memory.  SpMV units
+// run the CTA-per-item body (spmv_item.cuh) from an S-stage TMA ring that
+// keeps S claimed records in flight per CTA (S = 2..8; by default the
+// deepest ring that still allows the most CTAs per SM).  A CTA's shared memory is used by one
+// phase at a time (the queue order makes the phases disjoint, see the
+// kernel).  Every mbarrier wait is bounded; on expiry the
 // batch's error flag is set and the CTA waits (bounded) for its own copies
-// and leaves.
+// and leaves.  The SpMV split tiles of all matrices are combined by one
+// launch after the kernel (a second node of the graph).
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -74,90 +75,108 @@ __device__ __forceinline__ void run_spmm_unit(const BatchUnit U, const unsigned 
     }
 }
 
-__global__ void __launch_bounds__(SABLE_THREADS, 2)
+// Queue order puts every SpMM unit before every SpMV unit, and a CTA's claims
+// (atomicAdd on the head) only grow, so a CTA runs SpMM units until its first
+// SpMV claim and SpMV units from then on:
+//   phase 1  SpMM units straight from global memory, no copy in flight;
+//   phase 2  SpMV units through an S-stage ring: the CTA keeps S claimed units'
+//            records in flight (TMA bulk copies, one mbarrier per stage), waits
+//            for the oldest, computes it, and refills its stage with a new claim.
+// SPMM = false compiles the SpMV-only form (fewer registers, more CTAs per SM).
+template <int S, bool SPMM>
+__global__ void __launch_bounds__(SABLE_THREADS, SPMM ? 2 : 3)
 batch_kernel(const BatchArgs b) {
     extern __shared__ __align__(128) unsigned char smem[];
     float *red = reinterpret_cast<float *>(smem);
     float *ysw = red + RED_FLOATS;
-    unsigned char *stage[2] = {smem + STAGE_OFF, smem + STAGE_OFF + b.stage_bytes};
-    __shared__ __align__(8) unsigned long long s_bar[2];
-    __shared__ int s_cur, s_pref, s_next, s_next_pref, s_last;
+    unsigned char *const stage0 = smem + STAGE_OFF;
+    __shared__ __align__(8) unsigned long long s_bar[S];
+    __shared__ int s_unit[S];   // unit claimed into each stage (>= n_units: none)
+    __shared__ int s_claim;
+    __shared__ int s_bad;
     const int tid = threadIdx.x;
-    const unsigned bar[2] = {smem_addr(&s_bar[0]), smem_addr(&s_bar[1])};
-    unsigned phase[2] = {0u, 0u};  // control thread: parity of each stage's next wait
+    const int n = b.n_units;
+    unsigned phase_bits = 0;    // control thread: parity of each stage's next wait
+    auto bar = [&](int k) { return smem_addr(&s_bar[k]); };
+    auto stage = [&](int k) { return stage0 + (size_t)k * b.stage_bytes; };
+    // control thread: claim a unit for stage k and start its record copy
+    auto refill = [&](int k) {
+        const int u = atomicAdd(b.head, 1);
+        s_unit[k] = u;
+        if (u < n) {
+            const ItemRef r = b.items[b.units[u].item];
+            tma_record(bar(k), stage(k), b.records + r.off, (unsigned)r.bytes);
+        }
+    };
     if (tid == CTRL) {
-        mbar_init(bar[0]);
-        mbar_init(bar[1]);
+        for (int k = 0; k < S; ++k) mbar_init(bar(k));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        s_cur = atomicAdd(b.head, 1);
-        s_pref = 0;
+        s_claim = atomicAdd(b.head, 1);
+        s_bad = 0;
     }
     for (int i = tid; i < RED_FLOATS; i += SABLE_THREADS) ysw[i] = 0.f;
     __syncthreads();
-    int st = 0;  // stage of the next SpMV unit
-    while (true) {
-        const int u = s_cur;
-        const int pref = s_pref;
-        if (u >= b.n_units) break;
-        const BatchUnit U = b.units[u];
-        if (U.kind == U_SPMV) {
-            bool bad = false, landed = true;
-            int next_in_flight = 0;
-            const ItemRef ref = b.items[U.item];
-            if (tid == CTRL) {
-                if (!pref) tma_record(bar[st], stage[st], b.records + ref.off, (unsigned)ref.bytes);
-                const int un = atomicAdd(b.head, 1);
-                if (un < b.n_units) {
-                    const BatchUnit V = b.units[un];
-                    if (V.kind == U_SPMV) {
-                        const ItemRef r2 = b.items[V.item];
-                        tma_record(bar[st ^ 1], stage[st ^ 1], b.records + r2.off, (unsigned)r2.bytes);
-                        next_in_flight = 1;
-                    }
-                }
-                s_next = un;
-                s_next_pref = next_in_flight;
-                landed = mbar_wait(bar[st], phase[st]);
-                if (landed) phase[st] ^= 1u;
-                bad = !landed || reinterpret_cast<const ItemHeader *>(stage[st])->bytes != ref.bytes;
-            }
-            if (__syncthreads_or(bad)) {
-                if (tid == CTRL) {
-                    atomicExch(b.error, 1);
-                    if (!landed) mbar_wait(bar[st], phase[st]);
-                    if (next_in_flight) mbar_wait(bar[st ^ 1], phase[st ^ 1]);
-                }
-                return;
-            }
-            const unsigned char *R = stage[st];
-            const ItemHeader hd = *reinterpret_cast<const ItemHeader *>(R);
-            const MatIO &io = b.mats[hd.mat];
-            cta_accumulate(R, hd, io.x, nullptr, red, ysw);
-            __syncthreads();
-            cta_finish(hd, io, red, ysw, &s_last);
-            st ^= 1;
-        } else {
-            if (tid == CTRL) {
-                s_next = atomicAdd(b.head, 1);
-                s_next_pref = 0;
-            }
+
+    // ---- phase 1: SpMM units -------------------------------------------------
+    if (SPMM) {
+        while (true) {
+            const int u = s_claim;
+            if (u >= n || b.units[u].kind == U_SPMV) break;
+            const BatchUnit U = b.units[u];
             const ItemRef ref = b.items[U.item];
             const unsigned char *R = b.records + ref.off;
             if (reinterpret_cast<const ItemHeader *>(R)->bytes == ref.bytes) {
-                const MatIO &io = b.mats[reinterpret_cast<const ItemHeader *>(R)->mat];
-                run_spmm_unit(U, R, io, smem);
+                run_spmm_unit(U, R, b.mats[reinterpret_cast<const ItemHeader *>(R)->mat], smem);
             } else if (tid == CTRL) {
                 atomicExch(b.error, 1);
             }
             __syncthreads();
-            // the SpMM body used the whole shared memory: restore the zero CSR rows
-            for (int i = tid; i < RED_FLOATS; i += SABLE_THREADS) ysw[i] = 0.f;
+            if (tid == CTRL) s_claim = atomicAdd(b.head, 1);
+            __syncthreads();
+        }
+        // the SpMM bodies used the whole shared memory: restore the zero CSR rows
+        for (int i = tid; i < RED_FLOATS; i += SABLE_THREADS) ysw[i] = 0.f;
+        __syncthreads();
+    }
+
+    // ---- phase 2: SpMV ring --------------------------------------------------
+    if (s_claim >= n) return;
+    if (tid == CTRL) {
+        const int u0 = s_claim;
+        s_unit[0] = u0;
+        const ItemRef r = b.items[b.units[u0].item];
+        tma_record(bar(0), stage(0), b.records + r.off, (unsigned)r.bytes);
+        for (int k = 1; k < S; ++k) refill(k);
+    }
+    __syncthreads();
+    for (int it = 0;; ++it) {
+        const int k = it % S;
+        const int u = s_unit[k];
+        if (u >= n) break;
+        if (tid == CTRL) {
+            const bool landed = mbar_wait(bar(k), (phase_bits >> k) & 1u);
+            if (landed) phase_bits ^= 1u << k;
+            const ItemRef ref = b.items[b.units[u].item];
+            if (!landed || reinterpret_cast<const ItemHeader *>(stage(k))->bytes != ref.bytes) {
+                // flag, then wait (bounded) for every copy this CTA has in flight
+                atomicExch(b.error, 1);
+                for (int j = 0; j < S; ++j) {
+                    const int kk = (k + j) % S;
+                    if (s_unit[kk] < n && (kk != k || !landed)) mbar_wait(bar(kk), (phase_bits >> kk) & 1u);
+                }
+                s_bad = 1;
+            }
         }
         __syncthreads();
-        if (tid == CTRL) {
-            s_cur = s_next;
-            s_pref = s_next_pref;
-        }
+        if (s_bad) return;
+        const unsigned char *R = stage(k);
+        const ItemHeader hd = *reinterpret_cast<const ItemHeader *>(R);
+        const MatIO &io = b.mats[hd.mat];
+        cta_accumulate(R, hd, io.x, nullptr, red, ysw);
+        __syncthreads();
+        cta_finish(hd, io, red, ysw);
+        __syncthreads();   // stage k is free
+        if (tid == CTRL) refill(k);
         __syncthreads();
     }
 }
@@ -187,6 +206,20 @@ int spmm_unit_smem(int16_t kind) {
     }
 }
 
+using BatchKernel = void (*)(BatchArgs);
+
+// Instantiated ring depths: 2/4 with SpMM bodies, 2/3/4/6/8 SpMV-only.
+BatchKernel batch_kernel_for(int S, bool spmm) {
+    if (spmm) return S >= 4 ? batch_kernel<4, true> : batch_kernel<2, true>;
+    switch (S) {
+        case 2: return batch_kernel<2, false>;
+        case 3: return batch_kernel<3, false>;
+        case 4: return batch_kernel<4, false>;
+        case 6: return batch_kernel<6, false>;
+        default: return batch_kernel<8, false>;
+    }
+}
+
 }  // namespace
 
 struct sable_batch {
@@ -203,8 +236,11 @@ struct sable_batch {
     int *d_counters = nullptr;
     int *d_head = nullptr;
     int *d_error = nullptr;
+    SplitTile *d_splits = nullptr;       // SpMV split tiles of every matrix (combine launch)
+    int n_splits = 0;
     int64_t n_units = 0, device_bytes = 0;
-    int stage_bytes = 0, smem = 0, n_ctas = 0;
+    int stage_bytes = 0, smem = 0, n_ctas = 0, stages = 0;
+    BatchKernel kernel = nullptr;
     bool mats_valid = false;
     bool use_graph = false;
     cudaStream_t cap_stream = nullptr;
@@ -228,9 +264,15 @@ int batch_launch(sable_batch *bt, cudaStream_t s) {
     a.stage_bytes = bt->stage_bytes;
     cudaError_t e = cudaMemsetAsync(bt->d_head, 0, sizeof(int), s);
     if (e != cudaSuccess) return cuda_fail(e, "batch queue reset");
-    batch_kernel<<<bt->n_ctas, SABLE_THREADS, bt->smem, s>>>(a);
+    bt->kernel<<<bt->n_ctas, SABLE_THREADS, bt->smem, s>>>(a);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "batch kernel launch");
+    if (bt->n_splits > 0) {
+        MatIO none;
+        memset(&none, 0, sizeof none);
+        const int ec = launch_spmv_combine(bt->d_splits, bt->n_splits, bt->d_mats, none, s);
+        if (ec) return cuda_fail((cudaError_t)ec, "batch combine launch");
+    }
     return SABLE_OK;
 }
 
@@ -263,6 +305,7 @@ int sable_batch_destroy(sable_batch *bt) {
     cudaFree(bt->d_counters);
     cudaFree(bt->d_head);
     cudaFree(bt->d_error);
+    cudaFree(bt->d_splits);
     if (bt->h_mats) cudaFreeHost(bt->h_mats);
     if (prev >= 0) cudaSetDevice(prev);
     delete bt;
@@ -306,6 +349,7 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     items.reserve(n_items);
     item_mat.reserve(n_items);
     std::vector<MatIO> mats(n_plans);
+    std::vector<SplitTile> splits;
     struct Sortable {
         int32_t cls;
         int64_t cost;
@@ -354,6 +398,11 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
                 q.push_back(s);
             }
         }
+        if (W == 1)
+            for (SplitTile t : p->splits_host) {
+                t.mat = i;
+                splits.push_back(t);
+            }
         rec_base += p->records_bytes;
     }
     std::stable_sort(q.begin(), q.end(), [](const Sortable &a, const Sortable &b) {
@@ -368,7 +417,41 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     bt->n_units = (int64_t)units.size();
     if (bt->n_units >= INT32_MAX) return bail(fail(SABLE_ERR_UNSUPPORTED, "batch of %lld units", (long long)bt->n_units));
     bt->stage_bytes = (bt->stage_bytes + 127) & ~127;
-    bt->smem = std::max(bt->stage_bytes ? STAGE_OFF + 2 * bt->stage_bytes : 0, spmm_smem);
+    bool has_spmm = false;
+    for (const BatchUnit &u : units) has_spmm |= u.kind != U_SPMV;
+    int dev_max = 0, sms = 0;
+    cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, bt->device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, bt->device);
+    // ring depth: as asked, else the most CTAs per SM first (each CTA's compute
+    // is latency-bound, so concurrent CTAs matter more than depth), then the
+    // deepest ring at that CTA count
+    {
+        const int cand_spmm[] = {2, 4}, cand_spmv[] = {2, 3, 4, 6, 8};
+        const int *cand = has_spmm ? cand_spmm : cand_spmv;
+        const int ncand = has_spmm ? 2 : 5;
+        const int sm_budget = 227 * 1024;
+        int best_s = 2;
+        int64_t best_score = -1;
+        for (int c = 0; c < ncand; ++c) {
+            const int S = cand[c];
+            if (o.stages && S != o.stages) continue;
+            const int need = std::max(STAGE_OFF + S * bt->stage_bytes, spmm_smem);
+            if (need > dev_max) continue;
+            int per_sm = std::min(sm_budget / (need + 1024), has_spmm ? 2 : 3);
+            if (o.ctas_per_sm) per_sm = std::min(per_sm, o.ctas_per_sm);
+            if (per_sm < 1) continue;
+            const int64_t score = (int64_t)per_sm * 16 + S;
+            if (score > best_score) {
+                best_score = score;
+                best_s = S;
+            }
+        }
+        if (o.stages && best_score < 0)
+            return bail(fail(SABLE_ERR_UNSUPPORTED, "stages=%d does not fit shared memory", o.stages));
+        bt->stages = best_s;
+    }
+    bt->kernel = batch_kernel_for(bt->stages, has_spmm);
+    bt->smem = std::max(bt->stage_bytes ? STAGE_OFF + bt->stages * bt->stage_bytes : 0, spmm_smem);
     bt->smem = std::max(bt->smem, STAGE_OFF);
 
     int64_t &bytes = bt->device_bytes;
@@ -380,6 +463,8 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     if ((rc = dev_alloc(&bt->d_counters, (size_t)counter_total, &bytes, "counters"))) return bail(rc);
     if ((rc = dev_alloc(&bt->d_head, 1, &bytes, "queue head"))) return bail(rc);
     if ((rc = dev_alloc(&bt->d_error, 1, &bytes, "error flag"))) return bail(rc);
+    bt->n_splits = (int)splits.size();
+    if ((rc = dev_alloc(&bt->d_splits, splits.size(), &bytes, "split tiles"))) return bail(rc);
     int32_t *d_item_mat = nullptr;
     int64_t scratch_bytes = 0;
     if ((rc = dev_alloc(&d_item_mat, item_mat.size(), &scratch_bytes, "item matrices"))) return bail(rc);
@@ -396,6 +481,8 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
         e = cudaMemcpy(bt->d_units, units.data(), units.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(d_item_mat, item_mat.data(), item_mat.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !splits.empty())
+        e = cudaMemcpy(bt->d_splits, splits.data(), splits.size() * sizeof(SplitTile), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !items.empty()) {
         patch_mat_kernel<<<(unsigned)((items.size() + 255) / 256), 256>>>(bt->d_records, bt->d_items, d_item_mat,
                                                                           (int)items.size());
@@ -415,14 +502,12 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     memcpy(bt->h_mats, mats.data(), mats.size() * sizeof(MatIO));
 
     // launch shape
-    int dev_max = 0, sms = 0, occ = 0;
-    cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, bt->device);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, bt->device);
+    int occ = 0;
     if (bt->smem > dev_max)
         return bail(fail(SABLE_ERR_UNSUPPORTED, "batch needs %d bytes of shared memory per CTA (device: %d)", bt->smem,
                          dev_max));
-    e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bt->smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, SABLE_THREADS, bt->smem);
+    e = cudaFuncSetAttribute(bt->kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bt->smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, bt->kernel, SABLE_THREADS, bt->smem);
     if (e != cudaSuccess) return bail(cuda_fail(e, "batch kernel occupancy"));
     occ = std::max(occ, 1);
     const int per_sm = o.ctas_per_sm ? std::min(o.ctas_per_sm, occ) : occ;
@@ -510,6 +595,7 @@ int sable_batch_get_info(const sable_batch *bt, sable_batch_info *out) {
     out->device_bytes = bt->device_bytes;
     out->smem_bytes = bt->smem;
     out->stage_bytes = bt->stage_bytes;
+    out->stages = bt->stages;
     return SABLE_OK;
 }
 

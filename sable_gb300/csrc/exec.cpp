@@ -78,6 +78,9 @@ int plan_upload(sable_plan *p, const Layout &L) {
     if ((rc = upload_vec(&p->d_partial, part.data(), part.size(), "partial", &bytes))) return rc;
     std::vector<int> cnt((size_t)std::max<int32_t>(L.n_split_tiles, 1), 0);
     if ((rc = upload_vec(&p->d_counters, cnt.data(), cnt.size(), "counters", &bytes))) return rc;
+    p->splits_host = L.splits;
+    if (!L.splits.empty() && (rc = upload_vec(&p->d_splits, L.splits.data(), L.splits.size(), "split tiles", &bytes)))
+        return rc;
     std::vector<int> err(4, 0);
     if ((rc = upload_vec(&p->d_error, err.data(), err.size(), "error flag", &bytes))) return rc;
     int dev_max = 0;
@@ -130,6 +133,7 @@ static int run_spmv(sable_plan *p, const float *x, float *y, int64_t *cycles, vo
     int e;
     if (cycles || p->schedule == SABLE_SCHEDULE_ITEMS) {
         e = launch_spmv_items(a, cycles != nullptr, stream);
+        if (!e && p->n_split_tiles > 0) e = launch_spmv_combine(p->d_splits, p->n_split_tiles, nullptr, a.mat0, stream);
     } else {
         e = launch_spmv_warps(a, p->n_ctas, stream);
     }
@@ -247,6 +251,7 @@ int sable_plan_destroy(sable_plan *p) {
     cudaFree(p->d_pcounters);
     cudaFree(p->d_partial);
     cudaFree(p->d_counters);
+    cudaFree(p->d_splits);
     cudaFree(p->d_error);
     cudaFree(p->d_spmm_partial);
     cudaFree(p->d_spmm_counters);

@@ -273,6 +273,13 @@ int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, Layout 
             const int32_t sid = split_tiles++;
             const int64_t pbase = part_floats;
             part_floats += (int64_t)nitem * h;
+            SplitTile st;
+            st.part_base = pbase;
+            st.row0 = row0;
+            st.h = h;
+            st.nitem = nitem;
+            st.mat = 0;
+            L.splits.push_back(st);
             int32_t kidx = 0;
             for (int32_t k = 0; k < nd; ++k) {
                 const int64_t q0 = nq * k / nd, q1 = nq * (k + 1) / nd;

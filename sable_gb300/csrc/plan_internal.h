@@ -17,6 +17,7 @@ struct Layout {
     std::vector<int64_t> item_tile;       // tile of each item
     int64_t n_tiles = 0, n_partial = 0, dense_values = 0, dense_padded = 0, sparse_nnz = 0;
     int32_t n_split_tiles = 0;
+    std::vector<SplitTile> splits;        // split tiles (counter index order)
     int max_item_bytes = 0;
     int max_xg_floats = 0;      // largest 4 nq + ns over items
 };
@@ -49,6 +50,8 @@ struct sable_plan {
     int64_t n_parts = 0, n_multi = 0;
     float *d_partial = nullptr;
     int *d_counters = nullptr;
+    SplitTile *d_splits = nullptr;       // SpMV combine table
+    std::vector<SplitTile> splits_host;
     int *d_error = nullptr;
     int64_t n_items = 0, n_partial = 0;
     int32_t n_split_tiles = 0;

@@ -79,6 +79,15 @@ struct WorkRef {
 };
 static_assert(sizeof(WorkRef) == 48, "WorkRef must stay 48 bytes");
 
+// A tile cut into several SpMV items.  Its items store per-item row sums in
+// the matrix's partial buffer ([part_base + k h, +h) for item k); a separate
+// combine launch adds them in item order and writes y.
+struct SplitTile {
+    int64_t part_base;
+    int32_t row0, h, nitem, mat;
+};
+static_assert(sizeof(SplitTile) == 24, "SplitTile must stay 24 bytes");
+
 // One matrix of a launch: its operand / result and (SpMM) width.
 struct MatIO {
     const float *x;
@@ -109,6 +118,8 @@ struct LaunchArgs {
 
 namespace sable {
 int launch_spmv_items(const LaunchArgs &a, bool timed, void *stream);
+// y rows of split tiles from their items' partial sums (after the items ran).
+int launch_spmv_combine(const SplitTile *tiles, int n_tiles, const MatIO *mats, const MatIO &mat0, void *stream);
 int launch_spmv_warps(const LaunchArgs &a, int n_workers, void *stream);
 int spmv_items_smem(int stage_bytes, int xg_floats);
 int spmv_warp_smem(int stage_bytes, int xg_floats);

@@ -205,13 +205,13 @@ __device__ __forceinline__ void spmm_fp32_item(const unsigned char *R, const Mat
         else *reinterpret_cast<float4 *>(a.partial + pbase + (int64_t)i * NT + 4 * q) = v;
     }
     if (split) {
-        __threadfence();
+        // split-K arrival as in cta_finish: barrier, one gpu-scope acq_rel
+        // arrival, barrier; the last CTA reads the partials through L2
         __syncthreads();
         int *cnt = a.counters + (int64_t)slice * a.pad + c.tile;   // a.pad: split tiles per N-slice
-        if (tid == 0) s_last = (atomicAdd(cnt, 1) == c.nitem - 1);
+        if (tid == 0) s_last = (arrive_acq_rel(cnt) == c.nitem - 1);
         __syncthreads();
         if (s_last) {
-            __threadfence();
             const int64_t tb = (int64_t)slice * part_stride + c.part_base * NT;
             for (int t = tid; t < h * CQ; t += SABLE_THREADS) {
                 const int i = t / CQ, q = t - i * CQ, n = n0 + 4 * q;
@@ -456,13 +456,13 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
         else *reinterpret_cast<float4 *>(a.partial + pbase + (int64_t)i * NT + 4 * q) = v;
     }
     if (split) {
-        __threadfence();
+        // split-K arrival as in cta_finish: barrier, one gpu-scope acq_rel
+        // arrival, barrier; the last CTA reads the partials through L2
         __syncthreads();
         int *cnt = a.counters + (int64_t)slice * a.pad + c.tile;
-        if (tid == 0) s_last = (atomicAdd(cnt, 1) == c.nitem - 1);
+        if (tid == 0) s_last = (arrive_acq_rel(cnt) == c.nitem - 1);
         __syncthreads();
         if (s_last) {
-            __threadfence();
             const int64_t tb = (int64_t)slice * part_stride + c.part_base * NT;
             for (int e = tid; e < h * CQ; e += SABLE_THREADS) {
                 const int i = e / CQ, q = e - i * CQ, n = n0 + 4 * q;

@@ -41,7 +41,6 @@ spmv_items_kernel(const LaunchArgs a) {
     float *ysw = red + RED_FLOATS;
     unsigned char *stage = smem + STAGE_OFF;
     __shared__ __align__(8) unsigned long long s_bar;
-    __shared__ int s_last;
     const int tid = threadIdx.x;
     long long t0 = 0;
     if (TIMED && tid == 0) t0 = clock64();
@@ -73,11 +72,19 @@ spmv_items_kernel(const LaunchArgs a) {
     const MatIO &io = mat_of(a, hd.mat);
     cta_accumulate(stage, hd, io.x, nullptr, red, ysw);
     __syncthreads();
-    cta_finish(hd, io, red, ysw, &s_last);
+    cta_finish(hd, io, red, ysw);
     if (TIMED) {
         __syncthreads();
         if (tid == 0) a.cycles[blockIdx.x] = (int64_t)(clock64() - t0);
     }
+}
+
+__global__ void __launch_bounds__(256)
+spmv_combine_kernel(const SplitTile *__restrict__ tiles, int n, const MatIO *mats, const MatIO mat0) {
+    const int t = blockIdx.x * 8 + (threadIdx.x >> 5);
+    if (t >= n) return;
+    const SplitTile T = tiles[t];
+    combine_tile(T, mats ? mats[T.mat] : mat0, threadIdx.x & 31);
 }
 
 // ---------------------------------------------------------------------------
@@ -325,6 +332,12 @@ int launch_spmv_items(const LaunchArgs &a, bool timed, void *stream) {
         cudaFuncSetAttribute(spmv_items_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         spmv_items_kernel<false><<<a.n_items, SABLE_THREADS, smem, s>>>(a);
     }
+    return (int)cudaGetLastError();
+}
+
+int launch_spmv_combine(const SplitTile *tiles, int n_tiles, const MatIO *mats, const MatIO &mat0, void *stream) {
+    if (n_tiles <= 0) return 0;
+    spmv_combine_kernel<<<(n_tiles + 7) / 8, 256, 0, static_cast<cudaStream_t>(stream)>>>(tiles, n_tiles, mats, mat0);
     return (int)cudaGetLastError();
 }
 

@@ -4,8 +4,10 @@
 //   cta_accumulate  dense panel (lanes own rows, warps split the quads) into
 //                   red[warp][row], CSR entries (g lanes per row) into
 //                   ysw[warp][row]
-//   cta_finish      fixed-order row sums, output or split-tile partials, and
-//                   the last-arriving CTA's combine; leaves ysw zero.
+//   cta_finish      fixed-order row sums, output or split-tile partials;
+//                   leaves ysw zero
+//   combine_tile    y rows of a split tile from its items' partials (run by a
+//                   separate launch once all items are done).
 // Shared memory: red and ysw, RED_FLOATS floats each, ysw zero on entry.
 #pragma once
 #include "device_common.cuh"
@@ -109,11 +111,12 @@ __device__ __forceinline__ void cta_accumulate(const unsigned char *R, const Ite
     }
 }
 
-// Row sums in a fixed order, output, split-tile reduction; leaves ysw zero.
-__device__ __forceinline__ void cta_finish(const ItemHeader &hd, const MatIO &io, float *red, float *ysw, int *s_last) {
+// Row sums in a fixed order; a single-item tile writes y, an item of a split
+// tile stores its row sums as partials (the combine launch adds them).
+// Leaves ysw zero.
+__device__ __forceinline__ void cta_finish(const ItemHeader &hd, const MatIO &io, const float *red, float *ysw) {
     const int tid = threadIdx.x;
     const int h = hd.h;
-    const bool split = hd.nitem > 1;
     if (tid < h) {
         const int i = tid;
         float sd = 0.f;
@@ -133,22 +136,19 @@ __device__ __forceinline__ void cta_finish(const ItemHeader &hd, const MatIO &io
             ysw[w * SABLE_MAX_ROW_TILE + i] = 0.f;
         }
         const float tot = sd + sp;
-        if (!split) io.y[hd.row0 + i] = tot;
+        if (hd.nitem <= 1) io.y[hd.row0 + i] = tot;
         else io.partial[hd.part_base + (int64_t)hd.kidx * h + i] = tot;
     }
-    if (split) {
-        if (tid < h) __threadfence();  // this CTA's partial sums, visible at device scope
-        __syncthreads();
-        if (tid == CTRL) *s_last = (arrive_acq_rel(io.counters + hd.tile) == hd.nitem - 1);
-        __syncthreads();
-        if (*s_last) {
-            for (int i = tid; i < h; i += SABLE_THREADS) {
-                float s = 0.f;
-                for (int k = 0; k < hd.nitem; ++k) s += __ldcg(io.partial + hd.part_base + (int64_t)k * h + i);
-                io.y[hd.row0 + i] = s;
-            }
-            if (tid == CTRL) io.counters[hd.tile] = 0;  // ready for the next launch
-        }
+}
+
+// One warp per split tile: y rows = sum of the tile's item partials, in item
+// order (the same sum order on every run).
+__device__ __forceinline__ void combine_tile(const SplitTile &t, const MatIO &io, int lane) {
+    const float *P = io.partial + t.part_base;
+    for (int i = lane; i < t.h; i += 32) {
+        float s = 0.f;
+        for (int k = 0; k < t.nitem; ++k) s += P[(int64_t)k * t.h + i];
+        io.y[t.row0 + i] = s;
     }
 }
 
