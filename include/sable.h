@@ -86,6 +86,13 @@ typedef struct sable_plan_opts {
     int32_t schedule;     /* 0: one CTA per work item (TMA-staged record);
                              1: persistent warp workers over an LPT schedule
                              of tile parts, each with a private TMA ring       */
+    int32_t split_layout; /* a row tile larger than one work item is cut into
+                             0: items that each take a share of the tile's
+                                dense quads and of its CSR entries (SpMV runs
+                                both parts on separate warps side by side);
+                             1: dense items, then CSR items (better for SpMM,
+                                whose CTAs run the two parts one after the
+                                other)                                         */
 } sable_plan_opts;
 
 #define SABLE_TC_OFF    0

@@ -4,15 +4,20 @@ training data of the learned block cost model.
 The reference times every candidate block on the CPU, once as a dense
 kernel and once as CSR (studies/threshold.py:32-86), and fits its
 RandomForest to the faster label (studies/find_threshold.py:22-62).  Here
-the timings come from this library's own GPU kernels: a set of blocks is laid
-out as a block-diagonal VBR matrix (block k alone in block row k and block
-column k), so every work item of a plan belongs to exactly one block.  The
-matrix is planned twice, all blocks dense and all blocks sparse, and run with
-sable_spmv_timed / sable_spmm_timed, which record the SM cycles of every work
-item; a block's cost in one form is the sum over its items (median of
-`reps` launches).  Summed cycles are additive in the same way as the
-kernel's total time: it is the time of the items divided by the number of
-them that run at once.
+the timings come from this library's own GPU kernels.  A set of blocks is
+laid out so that sample block k has block row k to itself, together with a
+dense companion block of COMPANION_COLS columns in its own block column: in
+a real matrix a block shares its row tile with other blocks, and a work
+item's fixed cost (record copy, x loads, barriers) is shared by everything in
+it, so a block's cost only means something next to other work.  The matrix is
+planned twice, the sample blocks dense and the sample blocks sparse (the
+companions always dense), and run with sable_spmv_timed / sable_spmm_timed,
+which record the SM cycles of every work item; a block's cost in one form is
+the sum over the items of its block row (median of `reps` launches).  The
+companion adds the same work to both forms, so the comparison of the forms
+includes what the sparse form really adds to a tile: a CSR part beside the
+dense panel.  Summed cycles are additive like the kernel's total time: the
+time of the items divided by the number of them that run at once.
 """
 from __future__ import annotations
 
@@ -21,20 +26,38 @@ import numpy as np
 from . import convert, synth
 from .plan import Plan
 
-SPMM_TILE = 128  # widest N-slice of the SpMM kernels
+SPMM_TILE = 128       # widest N-slice of the SpMM kernels
+COMPANION_COLS = 64   # dense companion block beside every sample block
 
 
-def diag_vbr(blocks) -> synth.VbrMatrix:
-    """Block-diagonal VBR matrix of the given dense h x w float32 blocks."""
+def diag_vbr(blocks, companion_cols: int = 0, seed: int = 0) -> synth.VbrMatrix:
+    """VBR matrix with sample block k alone in block row k (block column 2k
+    when companions are on, k otherwise), plus, with companion_cols > 0, a
+    dense h x companion_cols block of U(-1, 1) values in block column 2k + 1."""
+    nb = len(blocks)
     hs = np.array([b.shape[0] for b in blocks], dtype=np.int64)
     ws = np.array([b.shape[1] for b in blocks], dtype=np.int64)
-    nb = len(blocks)
     rpntr = np.concatenate([[0], np.cumsum(hs)]).astype(np.int64)
-    cpntr = np.concatenate([[0], np.cumsum(ws)]).astype(np.int64)
-    indx = np.concatenate([[0], np.cumsum(hs * ws)]).astype(np.int64)
-    val = np.concatenate([np.asarray(b, np.float32).ravel(order="F") for b in blocks]) if nb else np.zeros(0, np.float32)
-    ar = np.arange(nb, dtype=np.int64)
-    return synth.VbrMatrix(val, indx, ar.copy(), rpntr, cpntr, ar.copy(), ar + 1)
+    if companion_cols <= 0:
+        cpntr = np.concatenate([[0], np.cumsum(ws)]).astype(np.int64)
+        indx = np.concatenate([[0], np.cumsum(hs * ws)]).astype(np.int64)
+        val = (np.concatenate([np.asarray(b, np.float32).ravel(order="F") for b in blocks]) if nb
+               else np.zeros(0, np.float32))
+        ar = np.arange(nb, dtype=np.int64)
+        return synth.VbrMatrix(val, indx, ar.copy(), rpntr, cpntr, ar.copy(), ar + 1)
+    rng = np.random.default_rng(seed)
+    widths = np.stack([ws, np.full(nb, companion_cols, np.int64)], 1).ravel()
+    cpntr = np.concatenate([[0], np.cumsum(widths)]).astype(np.int64)
+    sizes = np.stack([hs * ws, hs * companion_cols], 1).ravel()
+    indx = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    parts = []
+    for b in blocks:
+        parts.append(np.asarray(b, np.float32).ravel(order="F"))
+        parts.append(rng.uniform(-1, 1, b.shape[0] * companion_cols).astype(np.float32))
+    val = np.concatenate(parts) if nb else np.zeros(0, np.float32)
+    bindx = np.arange(2 * nb, dtype=np.int64)
+    bpntrb = 2 * np.arange(nb, dtype=np.int64)
+    return synth.VbrMatrix(val, indx, bindx, rpntr, cpntr, bpntrb, bpntrb + 2)
 
 
 def block_stats(blocks, N: int) -> np.ndarray:
@@ -54,12 +77,16 @@ def _slices(N: int) -> int:
     return (N + nt - 1) // nt
 
 
-def _form_cycles(m: synth.VbrMatrix, dense: bool, N: int, reps: int, spmm_tc, chunk_bytes: int) -> np.ndarray:
+def _form_cycles(m: synth.VbrMatrix, dense: bool, N: int, reps: int, spmm_tc, chunk_bytes: int,
+                 companions: bool) -> np.ndarray:
+    """Cycles of every block row (= sample block) with the samples in one form."""
     import torch
-    nb = m.n_blocks
-    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre,
-                            np.full(nb, dense, dtype=bool))
-    plan = Plan(comp, chunk_bytes=chunk_bytes, spmm_tc=spmm_tc)
+    nb = len(m.rpntr) - 1
+    mask = np.full(m.n_blocks, dense, dtype=bool)
+    if companions:
+        mask[1::2] = True
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mask)
+    plan = Plan(comp, chunk_bytes=chunk_bytes, spmm_tc=spmm_tc, split_layout="mixed" if N == 1 else "separate")
     try:
         n_items = plan.stats()["n_chunks"]
         tile_of = plan.chunk_tiles()
@@ -90,11 +117,14 @@ def _form_cycles(m: synth.VbrMatrix, dense: bool, N: int, reps: int, spmm_tc, ch
         plan.close()
 
 
-def time_blocks(blocks, N: int, reps: int = 5, spmm_tc="split3", chunk_bytes: int = 0):
-    """(dense cycles, sparse cycles) of every block, float64 [n_blocks] each."""
-    m = diag_vbr(blocks)
-    return (_form_cycles(m, True, N, reps, spmm_tc, chunk_bytes),
-            _form_cycles(m, False, N, reps, spmm_tc, chunk_bytes))
+def time_blocks(blocks, N: int, reps: int = 5, spmm_tc="split3", chunk_bytes: int = 0,
+                companion_cols: int = COMPANION_COLS):
+    """(dense cycles, sparse cycles) of every block in its block row (with its
+    companion), float64 [n_blocks] each."""
+    m = diag_vbr(blocks, companion_cols)
+    c = companion_cols > 0
+    return (_form_cycles(m, True, N, reps, spmm_tc, chunk_bytes, c),
+            _form_cycles(m, False, N, reps, spmm_tc, chunk_bytes, c))
 
 
 def matrix_blocks(m: synth.VbrMatrix):

@@ -150,7 +150,7 @@ static int collect_dense(const sable_vbrc_desc *d, std::vector<std::vector<Dense
 // ---------------------------------------------------------------------------
 static inline int64_t pad16(int64_t b) { return (b + 15) & ~(int64_t)15; }
 
-int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, Layout &L) {
+int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int split_layout, Layout &L) {
     std::vector<std::vector<DenseBlock>> rows;
     int rc = collect_dense(d, rows);
     if (rc) return rc;
@@ -266,10 +266,23 @@ int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, Layout 
                 emit_item(row0, h, 0, nq, 0, ns, k0, -1, 0, 1, 0);
                 continue;
             }
-            const int64_t qcap = std::max<int64_t>(1, (item_bytes - hdr) / (16 * ((int64_t)h + 1)));
-            const int64_t scap = std::max<int64_t>(2, (item_bytes - hdr - pad16(4 * ((int64_t)h + 1))) / 8) & ~(int64_t)1;
-            const int32_t nd = (int32_t)((nq + qcap - 1) / qcap), nsp = (int32_t)((ns + scap - 1) / scap);
-            const int32_t nitem = nd + nsp;
+            // Split tile.  Mixed layout: every item takes an equal share of the
+            // tile's quads and of its CSR entries (each item then mixes both
+            // parts like a tile that fits one item, and no item is CSR-only).
+            // Separate layout: dense items of the quads, then CSR items; each
+            // part alone exceeds an item whenever the tile is split, so
+            // nd + nsp >= 2.
+            const int64_t avail_d = std::max<int64_t>(1024, item_bytes - hdr);
+            const int64_t avail_s = std::max<int64_t>(1024, item_bytes - hdr - pad16(4 * ((int64_t)h + 1)) - 16);
+            int32_t nd = 0, nsp = 0, nitem;
+            if (split_layout == 0) {
+                const int64_t content = 16 * nq * ((int64_t)h + 1) + 8 * ns;
+                nitem = (int32_t)std::max<int64_t>(2, (content + avail_s - 1) / avail_s);
+            } else {
+                nd = (int32_t)((16 * nq * ((int64_t)h + 1) + avail_d - 1) / avail_d);
+                nsp = (int32_t)((8 * ns + avail_s - 1) / avail_s);
+                nitem = nd + nsp;
+            }
             const int32_t sid = split_tiles++;
             const int64_t pbase = part_floats;
             part_floats += (int64_t)nitem * h;
@@ -280,14 +293,18 @@ int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, Layout 
             st.nitem = nitem;
             st.mat = 0;
             L.splits.push_back(st);
-            int32_t kidx = 0;
-            for (int32_t k = 0; k < nd; ++k) {
-                const int64_t q0 = nq * k / nd, q1 = nq * (k + 1) / nd;
-                emit_item(row0, h, q0, q1, 0, 0, k0, sid, kidx++, nitem, pbase);
-            }
-            for (int32_t k = 0; k < nsp; ++k) {
-                const int64_t s0 = (ns * k / nsp) & ~(int64_t)0, s1 = ns * (k + 1) / nsp;
-                emit_item(row0, h, 0, 0, s0, s1, k0, sid, kidx++, nitem, pbase);
+            if (split_layout == 0) {
+                for (int32_t k = 0; k < nitem; ++k) {
+                    const int64_t q0 = nq * k / nitem, q1 = nq * (k + 1) / nitem;
+                    const int64_t s0 = ns * k / nitem, s1 = ns * (k + 1) / nitem;
+                    emit_item(row0, h, q0, q1, s0, s1, k0, sid, k, nitem, pbase);
+                }
+            } else {
+                int32_t kidx = 0;
+                for (int32_t k = 0; k < nd; ++k)
+                    emit_item(row0, h, nq * k / nd, nq * (k + 1) / nd, 0, 0, k0, sid, kidx++, nitem, pbase);
+                for (int32_t k = 0; k < nsp; ++k)
+                    emit_item(row0, h, 0, 0, ns * k / nsp, ns * (k + 1) / nsp, k0, sid, kidx++, nitem, pbase);
             }
         }
     }
@@ -392,7 +409,11 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
     }
     p->spmm_tc = o.spmm_tc;
     Layout L;
-    rc = build_layout(desc, row_tile, chunk_bytes, L);
+    if (o.split_layout != 0 && o.split_layout != 1) {
+        delete p;
+        return fail(SABLE_ERR_ARG, "split_layout %d unknown", o.split_layout);
+    }
+    rc = build_layout(desc, row_tile, chunk_bytes, o.split_layout, L);
     if (rc) { delete p; return rc; }
     rc = plan_upload(p, L);
     if (rc) { sable_plan_destroy(p); return rc; }
@@ -409,8 +430,10 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
     if (chunk_bytes < 4096 || chunk_bytes > SABLE_MAX_ITEM_BYTES * 4 / 5) return fail(SABLE_ERR_ARG, "chunk_bytes outside range");
     int rc = validate_vbrc(desc);
     if (rc) return rc;
+    const int split_layout = opts ? opts->split_layout : 0;
+    if (split_layout != 0 && split_layout != 1) return fail(SABLE_ERR_ARG, "split_layout %d unknown", split_layout);
     Layout L;
-    rc = build_layout(desc, row_tile, chunk_bytes, L);
+    rc = build_layout(desc, row_tile, chunk_bytes, split_layout, L);
     if (rc) return rc;
     memset(out, 0, sizeof *out);
     out->n_tiles = L.n_tiles;

@@ -26,7 +26,7 @@ int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 int set_device(int dev);
 int validate_vbrc(const sable_vbrc_desc *d);
-int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, Layout &L);
+int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int split_layout, Layout &L);
 int check_layout(const Layout &L);
 // Persistent schedule: tiles' items grouped into parts of <= part_bytes,
 // parts assigned to n_workers warp workers by greedy LPT (schedule.cpp).

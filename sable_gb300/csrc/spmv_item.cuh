@@ -68,13 +68,25 @@ __device__ __forceinline__ void cta_accumulate(const unsigned char *R, const Ite
     const float4 *P = reinterpret_cast<const float4 *>(R + hd.panel_off);
     const float4 *xg4 = reinterpret_cast<const float4 *>(xg);
     auto xq = [&](int q) { return xg ? xg4[q] : xquad(xc, q, x); };
+    // An item with both parts gives warps [0, wd) to the dense panel and
+    // warps [wd, NWARP) to the CSR entries, in proportion to their bytes, so
+    // the two latency chains run side by side; otherwise all warps take the
+    // one part there is.  The split depends only on the item: fixed sum order.
+    int wd = NWARP, wc = 0;
+    if (nq > 0 && ns > 0) {
+        const int64_t db = 16LL * nq * h, sb = 8LL * ns;
+        wd = (int)((NWARP * db + (db + sb) / 2) / (db + sb));
+        wd = min(max(wd, 1), NWARP - 1);
+        wc = wd;
+    }
+    const int dense_warps = nq > 0 ? wd : 0;
     if (h <= 32) {
         const int qpw = 32 / h;
         const bool act = lane < qpw * h;
         const int r = lane % h, s = lane / h;
         float acc = 0.f, accb = 0.f;
-        if (nq > 0 && act) {
-            const int step = NWARP * qpw;
+        if (warp < dense_warps && act) {
+            const int step = dense_warps * qpw;
             int q = warp * qpw + s;
             for (; q + step < nq; q += 2 * step) {
                 const float4 x0 = xq(q), x1 = xq(q + step);
@@ -87,7 +99,7 @@ __device__ __forceinline__ void cta_accumulate(const unsigned char *R, const Ite
     } else {
         float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
         const bool v1 = lane + 32 < h, v2 = lane + 64 < h, v3 = lane + 96 < h;
-        for (int q = warp; q < nq; q += NWARP) {
+        for (int q = warp; warp < dense_warps && q < nq; q += dense_warps) {
             const float4 xa = xq(q);
             const float4 *Pa = P + q * h + lane;
             acc0 = dot4(Pa[0], xa, acc0);
@@ -101,10 +113,11 @@ __device__ __forceinline__ void cta_accumulate(const unsigned char *R, const Ite
         if (v2) rw[lane + 64] = acc2;
         if (v3) rw[lane + 96] = acc3;
     }
-    if (ns > 0) {
+    if (ns > 0 && warp >= wc) {
         const int *rp = reinterpret_cast<const int *>(R + hd.rp_off);
         const uint2 *E = reinterpret_cast<const uint2 *>(R + hd.csr_off);
-        const int e_lo = (int)(((int64_t)ns * warp) / NWARP), e_hi = (int)(((int64_t)ns * (warp + 1)) / NWARP);
+        const int nwc = NWARP - wc, wi = warp - wc;
+        const int e_lo = (int)(((int64_t)ns * wi) / nwc), e_hi = (int)(((int64_t)ns * (wi + 1)) / nwc);
         const float *xe = xg ? xg + 4 * nq : nullptr;
         csr_rows(rp, E, h, hd.g, e_lo, e_hi, lane, ysw + warp * SABLE_MAX_ROW_TILE,
                  [&](int i, unsigned col) { return xe ? xe[i] : __ldg(x + col); });

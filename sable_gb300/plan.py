@@ -26,18 +26,19 @@ class Plan:
     """GPU plan of one compressed VBR matrix."""
 
     SCHEDULES = {"items": 0, "persistent": 1}
+    SPLIT_LAYOUTS = {"mixed": 0, "separate": 1}
     # dense-block SpMM precision for N >= 32: FP32 CUDA cores, or split BF16 on
     # the tensor cores with 2 terms (3 products) or 3 terms (6 products)
     TC_MODES = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, "off": 0, "split2": 1, "split3": 2}
 
     def __init__(self, comp: Compressed, row_tile: int = 0, chunk_bytes: int = 0, spmm_tc=False,
-                 device: int | None = None, schedule: str = "items"):
+                 device: int | None = None, schedule: str = "items", split_layout: str = "mixed"):
         lib = _lib.load()
         desc, keep = _lib.make_desc(comp)
         if spmm_tc not in self.TC_MODES:
             raise ValueError(f"spmm_tc {spmm_tc!r}: one of {sorted(map(str, self.TC_MODES))}")
         opts = _lib.PlanOpts(int(row_tile), int(chunk_bytes), self.TC_MODES[spmm_tc], -1 if device is None else int(device),
-                             self.SCHEDULES[schedule])
+                             self.SCHEDULES[schedule], self.SPLIT_LAYOUTS[split_layout])
         h = ctypes.c_void_p()
         _lib.check(lib.sable_plan_create(ctypes.byref(desc), ctypes.byref(opts), ctypes.byref(h)), "sable_plan_create")
         del keep
@@ -48,6 +49,7 @@ class Plan:
         self.row_tile = row_tile
         self.chunk_bytes = chunk_bytes
         self.schedule = schedule
+        self.split_layout = split_layout
 
     @property
     def handle(self) -> int:

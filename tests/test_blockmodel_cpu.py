@@ -18,6 +18,17 @@ def test_diag_layout_round_trip():
     assert all(np.array_equal(a, b) for a, b in zip(blocks, back))
 
 
+def test_companion_layout():
+    """Sample block k and its dense companion share block row k."""
+    blocks = sample_blocks(40)
+    m = blocktiming.diag_vbr(blocks, companion_cols=64)
+    convert.validate(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx)
+    assert m.n_blocks == 80 and m.n_cols == sum(b.shape[1] for b in blocks) + 64 * 40
+    back = blocktiming.matrix_blocks(m)
+    assert all(np.array_equal(a, back[2 * k]) for k, a in enumerate(blocks))
+    assert all(back[2 * k + 1].shape == (a.shape[0], 64) and np.all(back[2 * k + 1] != 0) for k, a in enumerate(blocks))
+
+
 def test_block_stats_match_feature_rows():
     blocks = sample_blocks(80)
     m = blocktiming.diag_vbr(blocks)

@@ -82,17 +82,18 @@ def test_block_features_match_numpy():
     np.testing.assert_allclose(out, ref, rtol=1e-6)
 
 
-def dry_run(comp, row_tile=0, chunk_bytes=0):
+def dry_run(comp, row_tile=0, chunk_bytes=0, split_layout=0):
     desc, keep = _lib.make_desc(comp)
     st = _lib.PlanStats()
-    opts = _lib.PlanOpts(row_tile, chunk_bytes, 0, -1, 0)
+    opts = _lib.PlanOpts(row_tile, chunk_bytes, 0, -1, 0, split_layout)
     _lib.check(_lib.load().sable_plan_dry_run(ctypes.byref(desc), ctypes.byref(opts), ctypes.byref(st)), "dry_run")
     return {k: getattr(st, k) for k, _ in st._fields_}
 
 
 @pytest.mark.parametrize("row_tile", [128, 64, 17, 1])
 @pytest.mark.parametrize("chunk_bytes", [0, 4096, 6000, 32768])
-def test_layout_builder_edge_shapes(row_tile, chunk_bytes):
+@pytest.mark.parametrize("split_layout", [0, 1])
+def test_layout_builder_edge_shapes(row_tile, chunk_bytes, split_layout):
     """Tall rows, width/height-1 partitions, empty rows, tiny work items:
     the builder's own bounds check (check_layout) passes and every stored
     value lands in the panel or the CSR segments exactly once."""
@@ -104,7 +105,7 @@ def test_layout_builder_edge_shapes(row_tile, chunk_bytes):
                        (r.random((h, w)) < 0.4))
     dense = rng.random(m.n_blocks) < 0.5
     comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense)
-    st = dry_run(comp, row_tile, chunk_bytes)
+    st = dry_run(comp, row_tile, chunk_bytes, split_layout)
     bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
     assert st["dense_values"] == int(bt.size[dense].sum())
     assert st["sparse_nnz"] == (0 if comp.indptr is None else int(comp.indptr[-1]))

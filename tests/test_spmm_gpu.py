@@ -67,11 +67,12 @@ def test_widths(cuda, N):
 
 @pytest.mark.parametrize("chunk_bytes", [0, 4096])
 @pytest.mark.parametrize("tc", [False, "split2", "split3"])
-def test_split_tiles_and_edges(cuda, chunk_bytes, tc):
+@pytest.mark.parametrize("split_layout", ["mixed", "separate"])
+def test_split_tiles_and_edges(cuda, chunk_bytes, tc, split_layout):
     m = random_vbr(6, [1, 300, 64, 2, 100], [1, 250, 3, 64, 77, 2, 31], 0.8)
     X = synth.dense_operand(m.n_cols, 64, 7)
     rng = np.random.default_rng(8)
-    Y, r = spmm_check(m, rng.random(m.n_blocks) < 0.5, X, tc=tc, chunk_bytes=chunk_bytes)
+    Y, r = spmm_check(m, rng.random(m.n_blocks) < 0.5, X, tc=tc, chunk_bytes=chunk_bytes, split_layout=split_layout)
     assert r["pass"], r
 
 

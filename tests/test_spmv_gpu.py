@@ -79,17 +79,18 @@ def test_spmv1000_vs_reference_c(golden, cuda, case, density):
 
 @pytest.mark.parametrize("row_tile", [128, 64, 17])
 @pytest.mark.parametrize("chunk_bytes", [0, 4096])
-@pytest.mark.parametrize("schedule", ["persistent", "items"])
-def test_edge_shapes(cuda, row_tile, chunk_bytes, schedule):
+@pytest.mark.parametrize("schedule,split_layout", [("persistent", "mixed"), ("items", "mixed"), ("items", "separate")])
+def test_edge_shapes(cuda, row_tile, chunk_bytes, schedule, split_layout):
     """Tall block rows (tile splits), width-1 / height-1 partitions, empty
-    block rows, tiny work items (split tiles, last-arriver reduction)."""
+    block rows, tiny work items (split tiles combined by the combine launch)."""
     rs = [1, 300, 5, 1, 64, 129, 7, 2, 40]
     cs = [1, 3, 200, 1, 9, 33, 128, 2, 4, 77]
     m = random_vbr(7, rs, cs, 0.6, empty_rows=(2,))
     x = synth.vector(m.n_cols, 8)
     rng = np.random.default_rng(9)
     dense = rng.random(m.n_blocks) < 0.5
-    plan, comp, y_ref, yabs = plan_and_ref(m, dense, x, row_tile=row_tile, chunk_bytes=chunk_bytes, schedule=schedule)
+    plan, comp, y_ref, yabs = plan_and_ref(m, dense, x, row_tile=row_tile, chunk_bytes=chunk_bytes, schedule=schedule,
+                                           split_layout=split_layout)
     y = run(plan, x)
     r = oracle.report(y, y_ref, yabs)
     assert r["pass"], r
