@@ -1,21 +1,31 @@
 #!/usr/bin/env python
-"""Benchmark: VBR SpMV on the 100000 x 100000 workload (GB/s, % of HBM roofline).
+"""Benchmark: VBR SpMV GB/s (headline), SpMM GFLOP/s and the mixed batch,
+learned+batched forms against the plain FP32 form, on one GB300.
 
-One step = one SpMV y = A x over the whole matrix (~2e4 blocks, ~5e7 stored
-values), x and A resident in HBM.  Each timed step is bracketed by CUDA
-events on the launching stream; a 256 MB buffer is written between steps to
-flush L2 (129 MB), outside the events.  Forms:
-
-  learned   per-block dense / sparse choice of the learned block model
-            (byte-cost rule until its weights are trained), plan kernel
-  plain     the reference's choice (its RandomForest), same kernel
-
-`value` is the learned form; `e2e` runs the same SpMV through the C ABI
-host-buffer entry (sable_spmv_host: pinned x copied in, y copied out, inside
-the timed region).  `--impl reference` times the reference's CPU executor
-(the oracle's C port of its generated code, FP64, all host cores) on the
-same workload.  Under torchrun each rank runs its own seeded replica (weak
-scaling, no collective on the data path).
+Headline step = one SpMV y = A x over the 100000 x 100000 workload (~2e4
+blocks of 10..100 rows/cols, ~5e7 stored values), x and A resident in HBM.
+Forms:
+  plain     the reference's block choice (its RandomForest threshold), plan
+            defaults (one CTA per 32 KB work item)
+  learned   the MLP cost model's block choice, launch shape picked by the
+            autotuner (tile height, work-item size, executor, ring depth)
+`value` = algorithmic bytes of the matrix (each block at its cheaper FP32
+encoding, plus x and y; sable_gb300.metrics) / time of the learned step,
+timed with CUDA events on the launching stream, L2 flushed (256 MB write)
+between steps outside the events.  `e2e` runs the same learned plan through
+the C ABI with host buffers (sable_spmv_host: pinned x copied in, y copied
+out, inside the timed region).  Also reported, each timed the same way:
+  spmm_50k   50000 x 50000, N = 32 and 128: plain = reference choice, FP32
+             CUDA cores; learned = MLP choice, split-BF16 tensor cores
+             (three terms, six products), autotuned; error vs FP64 (scipy
+             on the host) over a row sample
+  batch_256  256 matrices (half SpMV, half SpMM N = 64): plain = reference
+             choice, one launch per matrix, FP32; learned+batched = MLP
+             choice, one persistent-kernel graph launch
+`--impl reference` times the reference's CPU executor (the oracle's C port
+of its generated code, built with its compiler flags, FP64, all host cores)
+on the headline workload.  Under torchrun each rank runs its own seeded
+replica (weak scaling, no collective on the data path).
 """
 from __future__ import annotations
 
@@ -43,8 +53,8 @@ def peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d.get("bf16_tflops"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 class ClockSampler:
@@ -128,23 +138,24 @@ def barrier(world: int):
         dist.barrier()
 
 
+def choices(m, bt, N: int):
+    """(features, reference RandomForest choice, MLP choice) of a matrix at width N."""
+    from sable_gb300 import blockmodel, convert
+    feats = convert.block_features(m.val, bt, N)
+    rf = blockmodel.RFTableModel().choose_dense(feats)
+    mlp = blockmodel.MLPModel.load()
+    p = mlp.predict(feats)
+    return feats, rf, p[:, 0] < p[:, 1]
+
+
 def build_workload(rank: int):
-    from sable_gb300 import blockmodel, convert, metrics, synth
+    from sable_gb300 import convert, metrics, synth
     m = synth.spmv_100k(seed=synth.SEED_BASE + 1 + 100 * rank)
     x = synth.vector(m.n_cols, seed=31 + rank)
     bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
     nnz = convert.block_nnz(m.val, bt)
     B = metrics.spmv_matrix_bytes(bt, nnz) + 4 * (m.n_rows + m.n_cols)
-    feats = convert.block_features(m.val, bt, 1)
-    plain_choice = blockmodel.RFTableModel().choose_dense(feats)
-    learned_model = blockmodel.default_model()
-    if isinstance(learned_model, blockmodel.MLPModel):
-        learned_choice = learned_model.choose_dense(feats)
-        learned_name = "learned MLP cost model"
-    else:
-        learned_choice = 4 * bt.size <= 8 * nnz + 4 * (bt.h + 1)
-        learned_name = "byte-cost rule (block model weights absent)"
-    return m, x, bt, nnz, B, plain_choice, learned_choice, learned_name
+    return m, x, bt, nnz, B
 
 
 def time_device(fn, steps: int, warmup: int, world: int, flush):
@@ -171,46 +182,145 @@ def time_device(fn, steps: int, warmup: int, world: int, flush):
     return [s.elapsed_time(e) for s, e in evs]
 
 
+def bench_spmm(reps: int, flush) -> dict:
+    """50000^2 SpMM at N = 32 and 128: plain FP32 vs learned split-BF16 (autotuned)."""
+    import scipy.sparse
+    import torch
+    from sable_gb300 import autotune, convert, metrics, synth
+    from sable_gb300.plan import Plan
+    m = synth.spmm_50k()
+    bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+    nnz = int(convert.block_nnz(m.val, bt).sum())
+    out = {"workload": "spmm_50k: 50000x50000, 1000x1000 partitions in [20,80], block p=0.01, 60% dense blocks, "
+                       "rest density U[0.05,0.3], B 50000xN U(-1,1)", "nnz": nnz}
+    A64 = None
+    for N in (32, 128):
+        _, rf, mlp = choices(m, bt, N)
+        X = torch.as_tensor(synth.dense_operand(m.n_cols, N, 7)).cuda()
+        Y = torch.empty(m.n_rows, N, device="cuda")
+        comp_p = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, rf, bt=bt)
+        plain = Plan(comp_p, split_layout="separate")
+        ms_p = autotune.time_ms(lambda: plain.spmm(X, Y), reps)
+        comp_l = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mlp, bt=bt)
+        tuned = autotune.tune(comp_l, X, Y, N=N, spmm_tc="split3")
+        ms_l = autotune.time_ms(lambda: tuned.run(X, Y), reps)
+        tuned.run(X, Y)
+        Yl = Y.cpu().numpy().astype(np.float64)
+        # error against FP64 on the host (scipy CSR of A), 4000 sampled rows
+        if A64 is None:
+            rows, cols, vals = [], [], []
+            for k in range(len(bt.off)):
+                blk = np.asarray(m.val[bt.off[k]: bt.off[k] + bt.size[k]], np.float64).reshape(bt.w[k], bt.h[k]).T
+                r, c = np.nonzero(blk)
+                rows.append(r + bt.r0[k])
+                cols.append(c + bt.c0[k])
+                vals.append(blk[r, c])
+            A64 = scipy.sparse.csr_array((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                                         shape=(m.n_rows, m.n_cols))
+        sel = np.random.default_rng(5).choice(m.n_rows, 4000, replace=False)
+        Xh = X.cpu().numpy().astype(np.float64)
+        ref = A64[sel] @ Xh
+        scale = np.abs(A64[sel]) @ np.abs(Xh)
+        rel = np.abs(Yl[sel] - ref) / np.maximum(scale, 1e-300)
+        F = metrics.spmm_flops(m, N)
+        out[f"N{N}"] = {
+            "plain_fp32_gflops": round(F / (ms_p * 1e-3) / 1e9, 1), "plain_ms": round(ms_p, 4),
+            "learned_tc_gflops": round(F / (ms_l * 1e-3) / 1e9, 1), "learned_ms": round(ms_l, 4),
+            "learned_vs_plain": round(ms_p / ms_l, 3), "learned_config": tuned.config,
+            "error_vs_fp64_scaled": {"max": float(rel.max()), "median": float(np.median(rel)), "rows": 4000,
+                                     "precision": "split-BF16, three terms (hi+mid+lo), six products, FP32 accum"},
+            "dense_frac_learned": round(float(mlp.mean()), 3), "dense_frac_plain": round(float(rf.mean()), 3)}
+        plain.close()
+        tuned.close()
+    return out
+
+
+def bench_batch(reps: int) -> dict:
+    """256 mixed matrices: per-matrix launches (plain) vs one batched graph launch (learned)."""
+    import torch
+    from sable_gb300 import autotune, convert, synth
+    from sable_gb300.plan import Plan
+    mats, widths = synth.batch_256()
+    rng = np.random.default_rng(0)
+    xs, ys = [], []
+    for m, w in zip(mats, widths):
+        xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
+        ys.append(torch.empty(m.n_rows if w == 1 else (m.n_rows, w), device="cuda"))
+    plain, learned = [], []
+    nnz_work = 0
+    for m, w in zip(mats, widths):
+        bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+        f, rf, mlp = choices(m, bt, w)
+        nnz_work += int(f[:, 2].sum()) * w
+        lay = "mixed" if w == 1 else "separate"
+        plain.append(Plan(convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, rf, bt=bt),
+                          split_layout=lay))
+        learned.append(Plan(convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mlp,
+                                             bt=bt), spmm_tc="split3", split_layout=lay))
+
+    def run_plain():
+        for p, x, y, w in zip(plain, xs, ys, widths):
+            if w == 1:
+                p.spmv(x, y)
+            else:
+                p.spmm(x, y)
+
+    ms_p = autotune.time_ms(run_plain, reps)
+    batch, table = autotune.tune_batch(learned, widths, xs, ys)
+    ms_b = autotune.time_ms(lambda: batch.run(xs, ys), reps)
+    info = batch.info()
+    for p in plain + learned:
+        p.close()
+    batch.close()
+    return {"workload": "batch_256: 256 square matrices n log-U[1000,20000], partitions U[4,128], block p=0.02, "
+                        "dense fraction U[0.2,0.8], sparse density U[0.02,0.4]; SpMM N=64 for half",
+            "plain_ms": round(ms_p, 4), "plain_launches": len(mats) + sum(1 for w in widths if w == 1),
+            "learned_batched_ms": round(ms_b, 4), "learned_vs_plain": round(ms_p / ms_b, 3),
+            "work_gflop": round(2 * nnz_work / 1e9, 3), "learned_batched_gflops": round(2 * nnz_work / (ms_b * 1e6), 1),
+            "batch": {"n_units": info["n_units"], "n_ctas": info["n_ctas"], "stages": info["stages"],
+                      "graph": True, "tuning": table}}
+
+
 def run_sable(args):
     import torch
-    from sable_gb300 import convert
+    from sable_gb300 import _lib, autotune, blockmodel, convert
     from sable_gb300.plan import Plan
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
-    m, x, bt, nnz, B, plain_choice, learned_choice, learned_name = build_workload(rank)
+    m, x, bt, nnz, B = build_workload(rank)
+    feats, plain_choice, learned_choice = choices(m, bt, 1)
     comp_l = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, learned_choice, bt=bt)
     comp_p = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, plain_choice, bt=bt)
-    learned = Plan(comp_l)
     plain = Plan(comp_p)
     xd = torch.as_tensor(x).cuda()
     yd = torch.empty(m.n_rows, dtype=torch.float32, device="cuda")
+    learned = autotune.tune(comp_l, xd, yd, N=1)
     flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    flush = lambda: flush_buf.fill_(1)
+    flush = lambda: flush_buf.fill_(1)  # noqa: E731
 
     with ClockSampler(local) as clk:
-        t_learn = time_device(lambda: learned.spmv(xd, yd), args.steps, args.warmup, world, flush)
+        t_learn = time_device(lambda: learned.run(xd, yd), args.steps, args.warmup, world, flush)
     t_plain = time_device(lambda: plain.spmv(xd, yd), args.steps, args.warmup, world, flush)
-
     ms = max_over_ranks(statistics.mean(t_learn), world)
     ms_plain = max_over_ranks(statistics.mean(t_plain), world)
     value = world * B / (ms * 1e-3) / 1e9
     value_plain = world * B / (ms_plain * 1e-3) / 1e9
 
-    # end to end through the C ABI with host buffers (pinned)
+    # end to end through the C ABI with host buffers (pinned), learned plan
     xh = torch.as_tensor(x).pin_memory()
     yh = torch.empty(m.n_rows, dtype=torch.float32).pin_memory()
-    from sable_gb300 import _lib
     lib = _lib.load()
     stream = torch.cuda.current_stream().cuda_stream
+    e2e_plan = learned.plan
     for _ in range(args.warmup):
-        _lib.check(lib.sable_spmv_host(learned.handle, xh.data_ptr(), yh.data_ptr(), stream), "spmv_host")
+        _lib.check(lib.sable_spmv_host(e2e_plan.handle, xh.data_ptr(), yh.data_ptr(), stream), "spmv_host")
     barrier(world)
     e2e_t = []
     for _ in range(args.steps):
         flush()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        _lib.check(lib.sable_spmv_host(learned.handle, xh.data_ptr(), yh.data_ptr(), stream), "spmv_host")
+        _lib.check(lib.sable_spmv_host(e2e_plan.handle, xh.data_ptr(), yh.data_ptr(), stream), "spmv_host")
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(statistics.mean(e2e_t), world)
 
@@ -225,20 +335,26 @@ def run_sable(args):
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; no dataset)",
         "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MB write)",
-                   "choice": learned_name, "n_blocks": int(m.n_blocks), "stored_values": int(len(m.val)),
-                   "nnz": int(nnz.sum()), "bytes_per_step": int(B), "parallelism": f"replicas x{world}"},
+                   "choice": "learned MLP cost model (sable_gb300/models/block_cost_mlp.npz)",
+                   "launch_shape": learned.config, "n_blocks": int(m.n_blocks), "stored_values": int(len(m.val)),
+                   "nnz": int(nnz.sum()), "bytes_per_step": int(B), "dense_frac": round(float(learned_choice.mean()), 4),
+                   "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
-                     "peak_source": pk["source"]},
+                     "peak_source": pk["source"], "kernel": "spmv_items_kernel (+ split-tile combine) per step"},
         "e2e": {"value": round(world * B / e2e_s / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * m.n_cols,
                 "d2h_bytes_per_step": 4 * m.n_rows},
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * learned.launches_per_run(),
         "plain": {"value": round(value_plain, 2), "unit": "GB/s", "ms_per_step": round(ms_plain, 5),
                   "choice": "reference RandomForest (models/density_threshold_spmv.pkl)",
                   "frac": round(B / (statistics.mean(t_plain) * 1e-3) / 1e9 / pk["hbm_gbs"], 4)},
         "learned_vs_plain": round(ms_plain / ms, 3),
+        "autotune": learned.table,
         "clocks": clk.summary(),
     }
+    if rank == 0 and not args.quick:
+        out["spmm_50k"] = bench_spmm(10, flush)
+        out["batch_256"] = bench_batch(10)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(m, bt, plain_choice, x, B, seconds=args.cpu_seconds)
     if rank == 0:
@@ -252,7 +368,7 @@ def run_sable(args):
 
 def cpu_baseline(m, bt, choice, x, B, seconds: float = 15.0, threads: int | None = None) -> dict:
     """The reference's generated SpMV executor, as the oracle's C port (FP64,
-    its own block choice), on the host cores."""
+    its own block choice, its compiler flags), on the host cores."""
     from oracle import oracle
     from sable_gb300 import convert
     comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, choice, bt=bt,
@@ -263,7 +379,7 @@ def cpu_baseline(m, bt, choice, x, B, seconds: float = 15.0, threads: int | None
     iters = int(max(3, min(200, seconds / per)))
     t, used, _ = oracle.cpu_spmv_timed(comp, x, threads, iters)
     med = float(np.median(t)) * 1e-9
-    return {"value": round(B / med / 1e9, 3), "unit": "GB/s", "cores": int(threads), "kind": "port",
+    return {"value": round(B / med / 1e9, 3), "unit": "GB/s", "cores": int(used), "kind": "port",
             "sample": f"full 100000^2 matrix, {iters} SpMV iterations (median), FP64, reference block choice"}
 
 
@@ -273,8 +389,9 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle import oracle
-    from sable_gb300 import convert
-    m, x, bt, nnz, B, plain_choice, _, _ = build_workload(0)
+    from sable_gb300 import blockmodel, convert
+    m, x, bt, nnz, B = build_workload(0)
+    plain_choice = blockmodel.RFTableModel().choose_dense(convert.block_features(m.val, bt, 1))
     comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, plain_choice, bt=bt,
                             value_dtype=np.float64)
     threads = os.cpu_count() or 1
@@ -287,7 +404,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; no dataset)",
         "config": {"workload": WORKLOAD, "choice": "reference RandomForest", "bytes_per_step": int(B)},
-        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": int(threads), "kind": "port",
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": int(used), "kind": "port",
                          "sample": f"full matrix, {args.steps} timed SpMV iterations after {args.warmup} warm-up"},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -301,6 +418,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="sable", choices=["sable", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="headline SpMV only (no SpMM / batch sections)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -1,0 +1,152 @@
+"""Autotuner: picks the launch shape of a matrix by timing candidates on the GPU.
+
+For one compressed matrix and width N (1 = SpMV) it tries combinations of
+  row_tile      rows per tile (tile height)
+  chunk_bytes   matrix bytes per work item (tile width cut)
+  executor      "items" (one CTA per work item, plus the split-tile combine
+                launch) or "ring" (the persistent kernel of a one-matrix
+                batch, which keeps `stages` records in flight per CTA)
+  stages        ring depth, for the ring executor
+and keeps the fastest.  Every candidate is timed with CUDA events on the
+current stream, L2 flushed between runs (a 256 MB write), median of `reps`.
+The reference fixes its shape per matrix at code-generation time (one C
+function per matrix, src/codegen.py:293-452); this is the GPU counterpart of
+that specialisation step.  Results are cached in memory by a signature of the
+matrix structure and N.
+"""
+from __future__ import annotations
+
+import hashlib
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .batch import Batch
+from .convert import Compressed
+from .plan import Plan
+
+SPMV_CANDIDATES = [
+    {"executor": "items", "row_tile": 128, "chunk_bytes": cb} for cb in (16384, 32768, 49152)
+] + [
+    {"executor": "ring", "row_tile": 128, "chunk_bytes": cb, "stages": s} for cb in (16384, 32768) for s in (2, 3)
+]
+SPMM_CANDIDATES = [
+    {"executor": "items", "row_tile": rt, "chunk_bytes": cb} for rt in (128, 64) for cb in (16384, 32768)
+] + [{"executor": "ring", "row_tile": 128, "chunk_bytes": 32768, "stages": 2}]
+
+_cache: dict[str, dict] = {}
+
+
+def signature(comp: Compressed, N: int, spmm_tc) -> str:
+    h = hashlib.sha256()
+    for a in (comp.rpntr, comp.cpntr, comp.bpntrb, comp.bindx, comp.ublocks):
+        h.update(np.ascontiguousarray(a, dtype=np.int64).tobytes())
+    h.update(np.int64(0 if comp.indptr is None else comp.indptr[-1]).tobytes())
+    h.update(f"{N}/{spmm_tc}".encode())
+    return h.hexdigest()
+
+
+@dataclass
+class Tuned:
+    """A plan (and, for the ring executor, its one-matrix batch) in the chosen shape."""
+    config: dict
+    plan: Plan
+    batch: Batch | None = None
+    N: int = 1
+    table: list = field(default_factory=list)
+
+    def run(self, x, y, stream=None):
+        if self.batch is not None:
+            return self.batch.run([x], [y], stream)
+        return self.plan.spmv(x, y, stream) if self.N == 1 else self.plan.spmm(x, y, stream)
+
+    def launches_per_run(self) -> int:
+        """Kernels of this library per run (work items, plus the combine of split tiles)."""
+        splits = self.plan.stats()["scratch_floats"] > 0
+        return 1 + (1 if splits and self.N == 1 else 0)
+
+    def close(self):
+        if self.batch is not None:
+            self.batch.close()
+        self.plan.close()
+
+
+def _build(comp: Compressed, cfg: dict, N: int, spmm_tc) -> Tuned:
+    plan = Plan(comp, row_tile=cfg["row_tile"], chunk_bytes=cfg["chunk_bytes"], spmm_tc=spmm_tc,
+                split_layout="mixed" if N == 1 else "separate")
+    batch = None
+    if cfg["executor"] == "ring":
+        batch = Batch([plan], [N], use_graph=True, stages=cfg.get("stages", 0))
+    return Tuned(dict(cfg), plan, batch, N)
+
+
+def time_ms(fn, reps: int = 10, warmup: int = 3) -> float:
+    import torch
+    flush = torch.empty(256 << 20, dtype=torch.int8, device="cuda")
+    for _ in range(warmup):
+        fn()
+    ts = []
+    for _ in range(reps):
+        flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        fn()
+        e.record()
+        e.synchronize()
+        ts.append(s.elapsed_time(e))
+    return float(np.median(ts))
+
+
+def tune(comp: Compressed, x, y, N: int = 1, spmm_tc="split3", candidates=None, reps: int = 10,
+         use_cache: bool = True) -> Tuned:
+    """Time every candidate on (x, y) and return the fastest, built."""
+    key = signature(comp, N, spmm_tc)
+    if use_cache and key in _cache:
+        return _build(comp, _cache[key], N, spmm_tc)
+    cands = candidates or (SPMV_CANDIDATES if N == 1 else SPMM_CANDIDATES)
+    table, best, best_ms = [], None, float("inf")
+    for cfg in cands:
+        try:
+            t = _build(comp, cfg, N, spmm_tc)
+        except Exception as ex:  # a shape the device cannot hold (shared memory): skip it
+            table.append({**cfg, "ms": None, "error": str(ex)[:80]})
+            continue
+        ms = time_ms(lambda: t.run(x, y), reps)
+        t.plan.check()
+        if t.batch is not None:
+            t.batch.check()
+        table.append({**cfg, "ms": round(ms, 5)})
+        if ms < best_ms:
+            if best is not None:
+                best.close()
+            best, best_ms = t, ms
+        else:
+            t.close()
+    if best is None:
+        raise RuntimeError("no autotuner candidate could be built")
+    best.table = table
+    _cache[key] = best.config
+    return best
+
+
+def tune_batch(plans, widths, xs, ys, stages=(2, 4), reps: int = 10) -> tuple[Batch, list]:
+    """Pick the ring depth of a batch (CUDA graph on); returns (batch, table)."""
+    table, best, best_ms = [], None, float("inf")
+    for s in stages:
+        try:
+            b = Batch(plans, widths, use_graph=True, stages=s)
+        except Exception as ex:
+            table.append({"stages": s, "ms": None, "error": str(ex)[:80]})
+            continue
+        ms = time_ms(lambda: b.run(xs, ys), reps)
+        b.check()
+        table.append({"stages": s, "ms": round(ms, 5), "n_ctas": b.info()["n_ctas"]})
+        if ms < best_ms:
+            if best is not None:
+                best.close()
+            best, best_ms = b, ms
+        else:
+            b.close()
+    if best is None:
+        raise RuntimeError("no batch shape could be built")
+    return best, table
