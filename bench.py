@@ -32,6 +32,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import pathlib
 import statistics
 import subprocess
@@ -326,10 +327,11 @@ def run_sable(args):
 
     pk = peaks()
     achieved = B / (statistics.mean(t_learn) * 1e-3) / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "spmv_100k_traffic.json"
+    traffic = None   # DRAM bytes per launch of the work-item kernel, from the committed ncu summary
+    tf = ROOT / "profiles" / "spmv_items_kernel_spmv_100k.md"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get("learned_bytes_per_launch")
+        hit = re.search(r"traffic_bytes_per_launch:\s*(\d+)", tf.read_text())
+        traffic = int(hit.group(1)) if hit else None
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
