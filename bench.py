@@ -11,8 +11,10 @@ Forms:
             autotuner (tile height, work-item size, executor, ring depth)
 `value` = algorithmic bytes of the matrix (each block at its cheaper FP32
 encoding, plus x and y; sable_gb300.metrics) / time of the learned step,
-timed with CUDA events on the launching stream, L2 flushed (256 MB write)
-between steps outside the events.  `e2e` runs the same learned plan through
+timed with CUDA events on the launching stream, L2 flushed between steps
+outside the events (a 256 MB write, then a 256 MB read of a clean buffer, so
+that the step neither finds its data in L2 nor pays for writing back the
+flush's dirty lines).  `e2e` runs the same learned plan through
 the C ABI with host buffers (sable_spmv_host: pinned x copied in, y copied
 out, inside the timed region).  Also reported, each timed the same way:
   spmm_50k   50000 x 50000, N = 32 and 128: plain = reference choice, FP32
@@ -296,8 +298,7 @@ def run_sable(args):
     xd = torch.as_tensor(x).cuda()
     yd = torch.empty(m.n_rows, dtype=torch.float32, device="cuda")
     learned = autotune.tune(comp_l, xd, yd, N=1)
-    flush_buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    flush = lambda: flush_buf.fill_(1)  # noqa: E731
+    flush = autotune.l2_flush
 
     with ClockSampler(local) as clk:
         t_learn = time_device(lambda: learned.run(xd, yd), args.steps, args.warmup, world, flush)
@@ -336,7 +337,8 @@ def run_sable(args):
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; no dataset)",
-        "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MB write)",
+        "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MB write, then 256 MB read of a "
+                                               "clean buffer so no dirty lines are written back inside the step)",
                    "choice": "learned MLP cost model (sable_gb300/models/block_cost_mlp.npz)",
                    "launch_shape": learned.config, "n_blocks": int(m.n_blocks), "stored_values": int(len(m.val)),
                    "nnz": int(nnz.sum()), "bytes_per_step": int(B), "dense_frac": round(float(learned_choice.mean()), 4),

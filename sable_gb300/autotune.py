@@ -4,11 +4,12 @@ For one compressed matrix and width N (1 = SpMV) it tries combinations of
   row_tile      rows per tile (tile height)
   chunk_bytes   matrix bytes per work item (tile width cut)
   executor      "items" (one CTA per work item, plus the split-tile combine
-                launch) or "ring" (the persistent kernel of a one-matrix
-                batch, which keeps `stages` records in flight per CTA)
+                launch), "warp_items" (one warp per work item, SpMV only) or
+                "ring" (the persistent kernel of a one-matrix batch, which
+                keeps `stages` records in flight per CTA)
   stages        ring depth, for the ring executor
 and keeps the fastest.  Every candidate is timed with CUDA events on the
-current stream, L2 flushed between runs (a 256 MB write), median of `reps`.
+current stream, L2 flushed between runs (L2Flush), median of `reps`.
 The reference fixes its shape per matrix at code-generation time (one C
 function per matrix, src/codegen.py:293-452); this is the GPU counterpart of
 that specialisation step.  Results are cached in memory by a signature of the
@@ -27,6 +28,8 @@ from .plan import Plan
 
 SPMV_CANDIDATES = [
     {"executor": "items", "row_tile": 128, "chunk_bytes": cb} for cb in (16384, 32768, 49152)
+] + [
+    {"executor": "warp_items", "row_tile": rt, "chunk_bytes": cb} for rt in (8, 16, 32, 128) for cb in (8192, 16384, 32768)
 ] + [
     {"executor": "ring", "row_tile": 128, "chunk_bytes": cb, "stages": s} for cb in (16384, 32768) for s in (2, 3)
 ]
@@ -73,21 +76,46 @@ class Tuned:
 
 def _build(comp: Compressed, cfg: dict, N: int, spmm_tc) -> Tuned:
     plan = Plan(comp, row_tile=cfg["row_tile"], chunk_bytes=cfg["chunk_bytes"], spmm_tc=spmm_tc,
-                split_layout="mixed" if N == 1 else "separate")
+                split_layout="mixed" if N == 1 else "separate",
+                schedule="warp_items" if cfg["executor"] == "warp_items" else "items")
     batch = None
     if cfg["executor"] == "ring":
         batch = Batch([plan], [N], use_graph=True, stages=cfg.get("stages", 0))
     return Tuned(dict(cfg), plan, batch, N)
 
 
+class L2Flush:
+    """Between timed runs: write a 256 MB buffer (evicts everything of the run
+    before), then read a clean 256 MB buffer, so the run starts with L2 holding
+    neither its own data nor dirty lines whose write-back it would pay for."""
+
+    def __init__(self):
+        import torch
+        self.w = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        self.r = torch.ones(64 << 20, dtype=torch.float32, device="cuda")
+
+    def __call__(self):
+        self.w.fill_(1)
+        self.r.sum()
+
+
+_flush = None
+
+
+def l2_flush():
+    global _flush
+    if _flush is None:
+        _flush = L2Flush()
+    _flush()
+
+
 def time_ms(fn, reps: int = 10, warmup: int = 3) -> float:
     import torch
-    flush = torch.empty(256 << 20, dtype=torch.int8, device="cuda")
     for _ in range(warmup):
         fn()
     ts = []
     for _ in range(reps):
-        flush.zero_()
+        l2_flush()
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record()
         fn()

@@ -86,7 +86,8 @@ int plan_upload(sable_plan *p, const Layout &L) {
     int dev_max = 0;
     cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
     // Plans whose items are too large for a warp worker's ring run one CTA per item.
-    if (spmv_warp_smem(p->max_item_bytes, p->max_xg_floats) > dev_max) p->schedule = SABLE_SCHEDULE_ITEMS;
+    if (p->schedule == SABLE_SCHEDULE_PERSISTENT && spmv_warp_smem(p->max_item_bytes, p->max_xg_floats) > dev_max)
+        p->schedule = SABLE_SCHEDULE_ITEMS;
     if (spmv_items_smem(p->max_item_bytes, p->max_xg_floats + 4) > dev_max)
         return fail(SABLE_ERR_UNSUPPORTED, "work items need %d bytes of shared memory (device: %d)",
                     spmv_items_smem(p->max_item_bytes, p->max_xg_floats + 4), dev_max);
@@ -133,6 +134,9 @@ static int run_spmv(sable_plan *p, const float *x, float *y, int64_t *cycles, vo
     int e;
     if (cycles || p->schedule == SABLE_SCHEDULE_ITEMS) {
         e = launch_spmv_items(a, cycles != nullptr, stream);
+        if (!e && p->n_split_tiles > 0) e = launch_spmv_combine(p->d_splits, p->n_split_tiles, nullptr, a.mat0, stream);
+    } else if (p->schedule == SABLE_SCHEDULE_WARP_ITEMS) {
+        e = launch_spmv_warp_items(a, stream);
         if (!e && p->n_split_tiles > 0) e = launch_spmv_combine(p->d_splits, p->n_split_tiles, nullptr, a.mat0, stream);
     } else {
         e = launch_spmv_warps(a, p->n_ctas, stream);

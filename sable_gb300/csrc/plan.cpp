@@ -385,7 +385,9 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
     if (opts) o = *opts;
     const int row_tile = o.row_tile ? o.row_tile : SABLE_MAX_ROW_TILE;
     const int chunk_bytes = o.chunk_bytes ? o.chunk_bytes
-                                          : (o.schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES : SABLE_WARP_ITEM_BYTES);
+                                          : (o.schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES
+                                             : o.schedule == SABLE_SCHEDULE_WARP_ITEMS ? SABLE_WARP_ITEMS_ITEM_BYTES
+                                                                                       : SABLE_WARP_ITEM_BYTES);
     if (row_tile < 1 || row_tile > SABLE_MAX_ROW_TILE) return fail(SABLE_ERR_ARG, "row_tile %d outside 1..128", row_tile);
     if (chunk_bytes < 4096 || chunk_bytes > SABLE_MAX_ITEM_BYTES * 4 / 5)
         return fail(SABLE_ERR_ARG, "chunk_bytes %d outside 4096..%d", chunk_bytes, SABLE_MAX_ITEM_BYTES * 4 / 5);
@@ -398,7 +400,8 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
     cudaGetDevice(&p->device);
     p->row_tile = row_tile;
     p->item_bytes = chunk_bytes;
-    if (o.schedule != SABLE_SCHEDULE_ITEMS && o.schedule != SABLE_SCHEDULE_PERSISTENT) {
+    if (o.schedule != SABLE_SCHEDULE_ITEMS && o.schedule != SABLE_SCHEDULE_PERSISTENT &&
+        o.schedule != SABLE_SCHEDULE_WARP_ITEMS) {
         delete p;
         return fail(SABLE_ERR_ARG, "schedule %d unknown", o.schedule);
     }
@@ -425,7 +428,9 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
     if (!out) return fail(SABLE_ERR_ARG, "null output pointer");
     const int row_tile = opts && opts->row_tile ? opts->row_tile : SABLE_MAX_ROW_TILE;
     const int chunk_bytes = opts && opts->chunk_bytes ? opts->chunk_bytes
-                            : (!opts || opts->schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES : SABLE_WARP_ITEM_BYTES);
+                            : (!opts || opts->schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES
+                               : opts->schedule == SABLE_SCHEDULE_WARP_ITEMS ? SABLE_WARP_ITEMS_ITEM_BYTES
+                                                                             : SABLE_WARP_ITEM_BYTES);
     if (row_tile < 1 || row_tile > SABLE_MAX_ROW_TILE) return fail(SABLE_ERR_ARG, "row_tile %d outside 1..128", row_tile);
     if (chunk_bytes < 4096 || chunk_bytes > SABLE_MAX_ITEM_BYTES * 4 / 5) return fail(SABLE_ERR_ARG, "chunk_bytes outside range");
     int rc = validate_vbrc(desc);

@@ -36,6 +36,8 @@
 #define SABLE_WARP_ITEM_BYTES 8192   // default item size, warp workers
 #define SABLE_SCHEDULE_ITEMS 0
 #define SABLE_SCHEDULE_PERSISTENT 1
+#define SABLE_SCHEDULE_WARP_ITEMS 2
+#define SABLE_WARP_ITEMS_ITEM_BYTES 16384  // default item size, one warp per item
 
 struct __align__(16) ItemHeader {
     int32_t row0;       // first output row of the tile
@@ -118,6 +120,7 @@ struct LaunchArgs {
 
 namespace sable {
 int launch_spmv_items(const LaunchArgs &a, bool timed, void *stream);
+int launch_spmv_warp_items(const LaunchArgs &a, void *stream);
 // y rows of split tiles from their items' partial sums (after the items ran).
 int launch_spmv_combine(const SplitTile *tiles, int n_tiles, const MatIO *mats, const MatIO &mat0, void *stream);
 int launch_spmv_warps(const LaunchArgs &a, int n_workers, void *stream);

@@ -79,6 +79,105 @@ spmv_items_kernel(const LaunchArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// One warp per work item (schedule 2).  The record is read straight from HBM
+// with coalesced 16-byte streaming loads: no shared-memory staging, no TMA
+// wait and no CTA barrier, so every warp of the SM is an independent stream
+// and the SM keeps as many loads in flight as it has warps.  Dense panel:
+// for h <= 32 a warp step covers floor(32/h) quads (lane = (row, quad
+// offset)), for h > 32 lanes own rows lane, lane+32, ...; four quads per
+// step, their loads issued before any is used.  CSR entries: g lanes per row
+// into a per-warp row buffer in shared memory (warp-synchronous only).
+// ---------------------------------------------------------------------------
+constexpr int WI_WARPS = 8;
+
+__device__ __forceinline__ float4 ld_stream(const float4 *p) { return __ldcs(p); }
+
+__global__ void __launch_bounds__(WI_WARPS * 32, 4)
+spmv_warp_items_kernel(const LaunchArgs a) {
+    __shared__ float s_rows[WI_WARPS][SABLE_MAX_ROW_TILE];  // CSR row sums of each warp's item
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int item = blockIdx.x * WI_WARPS + w;
+    if (item >= a.n_items) return;  // the whole warp leaves; no CTA barrier follows
+    const ItemRef ref = a.items[item];
+    const unsigned char *R = a.records + ref.off;
+    const ItemHeader hd = *reinterpret_cast<const ItemHeader *>(R);
+    if (hd.bytes != ref.bytes || hd.h < 1 || hd.h > SABLE_MAX_ROW_TILE) {
+        if (lane == 0) atomicExch(a.error, 1);
+        return;
+    }
+    const MatIO &io = mat_of(a, hd.mat);
+    const float *__restrict__ x = io.x;
+    const int h = hd.h, nq = hd.nq, ns = hd.ns;
+    const int4 *xc = reinterpret_cast<const int4 *>(R + hd.xcol_off);
+    const float4 *P = reinterpret_cast<const float4 *>(R + hd.panel_off);
+    float *rows = s_rows[w];
+    for (int i = lane; i < h; i += 32) rows[i] = 0.f;
+    __syncwarp();
+    if (ns > 0) {
+        const int *rp = reinterpret_cast<const int *>(R + hd.rp_off);
+        const uint2 *E = reinterpret_cast<const uint2 *>(R + hd.csr_off);
+        csr_rows(rp, E, h, hd.g, 0, ns, lane, rows, [&](int, unsigned col) { return __ldg(x + col); });
+    }
+    auto put = [&](int i, float v) {
+        if (hd.nitem <= 1) io.y[hd.row0 + i] = v;
+        else io.partial[hd.part_base + (int64_t)hd.kidx * h + i] = v;
+    };
+    if (h <= 32) {
+        const int qpw = 32 / h, r = lane % h, sidx = lane / h;
+        float a0 = 0.f, a1 = 0.f;
+        if (lane < qpw * h) {
+            int q = sidx;
+            for (; q + 3 * qpw < nq; q += 4 * qpw) {
+                const float4 p0 = ld_stream(P + q * h + r), p1 = ld_stream(P + (q + qpw) * h + r);
+                const float4 p2 = ld_stream(P + (q + 2 * qpw) * h + r), p3 = ld_stream(P + (q + 3 * qpw) * h + r);
+                const float4 x0 = xquad(xc, q, x), x1 = xquad(xc, q + qpw, x);
+                const float4 x2 = xquad(xc, q + 2 * qpw, x), x3 = xquad(xc, q + 3 * qpw, x);
+                a0 = dot4(p0, x0, a0);
+                a1 = dot4(p1, x1, a1);
+                a0 = dot4(p2, x2, a0);
+                a1 = dot4(p3, x3, a1);
+            }
+            for (; q < nq; q += qpw) a0 = dot4(ld_stream(P + q * h + r), xquad(xc, q, x), a0);
+        }
+        const float v = a0 + a1;
+        float tot = 0.f;
+        for (int k = 0; k < qpw; ++k) tot += __shfl_sync(FULL, v, r + k * h);  // fixed order over the quad offsets
+        __syncwarp();
+        if (lane < h) put(lane, tot + rows[lane]);
+    } else {
+        const bool v1 = lane + 32 < h, v2 = lane + 64 < h, v3 = lane + 96 < h;
+        float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+        int q = 0;
+        for (; q + 1 < nq; q += 2) {
+            const float4 xa = xquad(xc, q, x), xb = xquad(xc, q + 1, x);
+            const float4 *Pa = P + q * h + lane, *Pb = Pa + h;
+            const float4 pa0 = ld_stream(Pa), pb0 = ld_stream(Pb);
+            float4 pa1 = make_float4(0.f, 0.f, 0.f, 0.f), pb1 = pa1, pa2 = pa1, pb2 = pa1, pa3 = pa1, pb3 = pa1;
+            if (v1) { pa1 = ld_stream(Pa + 32); pb1 = ld_stream(Pb + 32); }
+            if (v2) { pa2 = ld_stream(Pa + 64); pb2 = ld_stream(Pb + 64); }
+            if (v3) { pa3 = ld_stream(Pa + 96); pb3 = ld_stream(Pb + 96); }
+            c0 = dot4(pb0, xb, dot4(pa0, xa, c0));
+            c1 = dot4(pb1, xb, dot4(pa1, xa, c1));
+            c2 = dot4(pb2, xb, dot4(pa2, xa, c2));
+            c3 = dot4(pb3, xb, dot4(pa3, xa, c3));
+        }
+        if (q < nq) {
+            const float4 xa = xquad(xc, q, x);
+            const float4 *Pa = P + q * h + lane;
+            c0 = dot4(ld_stream(Pa), xa, c0);
+            if (v1) c1 = dot4(ld_stream(Pa + 32), xa, c1);
+            if (v2) c2 = dot4(ld_stream(Pa + 64), xa, c2);
+            if (v3) c3 = dot4(ld_stream(Pa + 96), xa, c3);
+        }
+        __syncwarp();
+        put(lane, c0 + rows[lane]);
+        if (v1) put(lane + 32, c1 + rows[lane + 32]);
+        if (v2) put(lane + 64, c2 + rows[lane + 64]);
+        if (v3) put(lane + 96, c3 + rows[lane + 96]);
+    }
+}
+
 __global__ void __launch_bounds__(256)
 spmv_combine_kernel(const SplitTile *__restrict__ tiles, int n, const MatIO *mats, const MatIO mat0) {
     const int t = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -332,6 +431,13 @@ int launch_spmv_items(const LaunchArgs &a, bool timed, void *stream) {
         cudaFuncSetAttribute(spmv_items_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         spmv_items_kernel<false><<<a.n_items, SABLE_THREADS, smem, s>>>(a);
     }
+    return (int)cudaGetLastError();
+}
+
+int launch_spmv_warp_items(const LaunchArgs &a, void *stream) {
+    if (a.n_items <= 0) return 0;
+    spmv_warp_items_kernel<<<(a.n_items + WI_WARPS - 1) / WI_WARPS, WI_WARPS * 32, 0,
+                             static_cast<cudaStream_t>(stream)>>>(a);
     return (int)cudaGetLastError();
 }
 

@@ -25,7 +25,7 @@ def _stream_handle(stream) -> int | None:
 class Plan:
     """GPU plan of one compressed VBR matrix."""
 
-    SCHEDULES = {"items": 0, "persistent": 1}
+    SCHEDULES = {"items": 0, "persistent": 1, "warp_items": 2}
     SPLIT_LAYOUTS = {"mixed": 0, "separate": 1}
     # dense-block SpMM precision for N >= 32: FP32 CUDA cores, or split BF16 on
     # the tensor cores with 2 terms (3 products) or 3 terms (6 products)

@@ -79,7 +79,8 @@ def test_spmv1000_vs_reference_c(golden, cuda, case, density):
 
 @pytest.mark.parametrize("row_tile", [128, 64, 17])
 @pytest.mark.parametrize("chunk_bytes", [0, 4096])
-@pytest.mark.parametrize("schedule,split_layout", [("persistent", "mixed"), ("items", "mixed"), ("items", "separate")])
+@pytest.mark.parametrize("schedule,split_layout", [("persistent", "mixed"), ("items", "mixed"), ("items", "separate"),
+                                                   ("warp_items", "mixed"), ("warp_items", "separate")])
 def test_edge_shapes(cuda, row_tile, chunk_bytes, schedule, split_layout):
     """Tall block rows (tile splits), width-1 / height-1 partitions, empty
     block rows, tiny work items (split tiles combined by the combine launch)."""
@@ -106,12 +107,13 @@ def test_all_dense_all_sparse(cuda, dense_all):
     assert oracle.report(y, y_ref, yabs)["pass"]
 
 
-def test_one_huge_block_row(cuda):
+@pytest.mark.parametrize("schedule", ["items", "warp_items"])
+def test_one_huge_block_row(cuda, schedule):
     """One block row with many blocks: dozens of work items on one tile."""
     m = random_vbr(13, [96], np.full(400, 50), 0.9, dense_frac=0.7)
     x = synth.vector(m.n_cols, 14)
     rng = np.random.default_rng(15)
-    plan, comp, y_ref, yabs = plan_and_ref(m, rng.random(m.n_blocks) < 0.6, x)
+    plan, comp, y_ref, yabs = plan_and_ref(m, rng.random(m.n_blocks) < 0.6, x, schedule=schedule)
     assert plan.stats()["n_chunks"] > 20
     y = run(plan, x)
     assert oracle.report(y, y_ref, yabs)["pass"]
@@ -144,7 +146,8 @@ def test_spmv_100k_full_size(cuda):
     nnz = convert.block_nnz(m.val, bt)
     cheaper_dense = 4 * bt.size <= 8 * nnz + 4 * (bt.h + 1)
     for dense, schedule in ((cheaper_dense, "persistent"), (np.zeros(m.n_blocks, bool), "persistent"),
-                            (cheaper_dense, "items")):
+                            (cheaper_dense, "items"), (cheaper_dense, "warp_items"),
+                            (np.ones(m.n_blocks, bool), "warp_items")):
         plan, comp, y_ref, yabs = plan_and_ref(m, dense, x, schedule=schedule)
         y = run(plan, x)
         r = oracle.report(y, y_ref, yabs)
