@@ -157,7 +157,8 @@ int sable_spmm_host(sable_plan *plan, const float *X_host, float *Y_host, int32_
 int sable_spmm_noalloc(sable_plan *plan, const float *X_dev, int64_t ldx, float *Y_dev, int64_t ldy,
                        int32_t N, void *stream);
 
-/* Per-work-item device time (SM clock cycles) of one SpMV / SpMM launch,
+/* Per-work-item device time (SM clock cycles) of one SpMV / SpMM launch
+ * (SpMV: one CTA per item, or one warp per item for plans of schedule 2),
  * written to cycles_dev[n_chunks] (SpMM: [n_slices][n_chunks]); used to
  * time blocks for the learned block model (the GPU counterpart of
  * studies/threshold.py:32-86). */

@@ -78,7 +78,7 @@ def _slices(N: int) -> int:
 
 
 def _form_cycles(m: synth.VbrMatrix, dense: bool, N: int, reps: int, spmm_tc, chunk_bytes: int,
-                 companions: bool) -> np.ndarray:
+                 companions: bool, schedule: str = "items", row_tile: int = 128) -> np.ndarray:
     """Cycles of every block row (= sample block) with the samples in one form."""
     import torch
     nb = len(m.rpntr) - 1
@@ -86,12 +86,14 @@ def _form_cycles(m: synth.VbrMatrix, dense: bool, N: int, reps: int, spmm_tc, ch
     if companions:
         mask[1::2] = True
     comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mask)
-    plan = Plan(comp, chunk_bytes=chunk_bytes, spmm_tc=spmm_tc, split_layout="mixed" if N == 1 else "separate")
+    plan = Plan(comp, chunk_bytes=chunk_bytes, spmm_tc=spmm_tc, split_layout="mixed" if N == 1 else "separate",
+                schedule=schedule if N == 1 else "items", row_tile=row_tile if N == 1 else 128)
     try:
         n_items = plan.stats()["n_chunks"]
         tile_of = plan.chunk_tiles()
         h = np.diff(m.rpntr)
-        tile_block = np.repeat(np.arange(nb), (h + 127) // 128)   # tiles of block row k (row tile 128)
+        rt = row_tile if N == 1 else 128
+        tile_block = np.repeat(np.arange(nb), (h + rt - 1) // rt)   # tiles of block row k
         item_block = tile_block[tile_of]
         rng = np.random.default_rng(nb)
         if N == 1:
@@ -117,14 +119,26 @@ def _form_cycles(m: synth.VbrMatrix, dense: bool, N: int, reps: int, spmm_tc, ch
         plan.close()
 
 
+# SpMV blocks are timed in the shape the autotuner picks for large matrices:
+# one warp per 32 KB work item, 8-row tiles.
+SPMV_SCHEDULE = "warp_items"
+SPMV_ROW_TILE = 8
+SPMV_CHUNK = 32768
+
+
 def time_blocks(blocks, N: int, reps: int = 5, spmm_tc="split3", chunk_bytes: int = 0,
                 companion_cols: int = COMPANION_COLS):
     """(dense cycles, sparse cycles) of every block in its block row (with its
     companion), float64 [n_blocks] each."""
     m = diag_vbr(blocks, companion_cols)
     c = companion_cols > 0
-    return (_form_cycles(m, True, N, reps, spmm_tc, chunk_bytes, c),
-            _form_cycles(m, False, N, reps, spmm_tc, chunk_bytes, c))
+    if N == 1:
+        kw = {"schedule": SPMV_SCHEDULE, "row_tile": SPMV_ROW_TILE}
+        cb = chunk_bytes or SPMV_CHUNK
+    else:
+        kw, cb = {}, chunk_bytes
+    return (_form_cycles(m, True, N, reps, spmm_tc, cb, c, **kw),
+            _form_cycles(m, False, N, reps, spmm_tc, cb, c, **kw))
 
 
 def matrix_blocks(m: synth.VbrMatrix):

@@ -120,7 +120,7 @@ struct LaunchArgs {
 
 namespace sable {
 int launch_spmv_items(const LaunchArgs &a, bool timed, void *stream);
-int launch_spmv_warp_items(const LaunchArgs &a, void *stream);
+int launch_spmv_warp_items(const LaunchArgs &a, bool timed, void *stream);
 // y rows of split tiles from their items' partial sums (after the items ran).
 int launch_spmv_combine(const SplitTile *tiles, int n_tiles, const MatIO *mats, const MatIO &mat0, void *stream);
 int launch_spmv_warps(const LaunchArgs &a, int n_workers, void *stream);
