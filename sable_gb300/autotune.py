@@ -64,9 +64,12 @@ class Tuned:
         return self.plan.spmv(x, y, stream) if self.N == 1 else self.plan.spmm(x, y, stream)
 
     def launches_per_run(self) -> int:
-        """Kernels of this library per run (work items, plus the combine of split tiles)."""
+        """Kernels of this library per run (work items, plus the combine of
+        split tiles for the per-CTA executors; the per-warp kernel combines
+        them itself)."""
         splits = self.plan.stats()["scratch_floats"] > 0
-        return 1 + (1 if splits and self.N == 1 else 0)
+        extra = splits and self.N == 1 and self.config["executor"] != "warp_items"
+        return 1 + (1 if extra else 0)
 
     def close(self):
         if self.batch is not None:

@@ -133,8 +133,7 @@ static int run_spmv(sable_plan *p, const float *x, float *y, int64_t *cycles, vo
     LaunchArgs a = spmv_args(p, x, y, cycles);
     int e;
     if (p->schedule == SABLE_SCHEDULE_WARP_ITEMS) {
-        e = launch_spmv_warp_items(a, cycles != nullptr, stream);
-        if (!e && p->n_split_tiles > 0) e = launch_spmv_combine(p->d_splits, p->n_split_tiles, nullptr, a.mat0, stream);
+        e = launch_spmv_warp_items(a, cycles != nullptr, stream);  // combines split tiles itself
     } else if (cycles || p->schedule == SABLE_SCHEDULE_ITEMS) {
         e = launch_spmv_items(a, cycles != nullptr, stream);
         if (!e && p->n_split_tiles > 0) e = launch_spmv_combine(p->d_splits, p->n_split_tiles, nullptr, a.mat0, stream);

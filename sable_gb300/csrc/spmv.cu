@@ -87,7 +87,9 @@ spmv_items_kernel(const LaunchArgs a) {
 // for h <= 32 a warp step covers floor(32/h) quads (lane = (row, quad
 // offset)), for h > 32 lanes own rows lane, lane+32, ...; four quads per
 // step, their loads issued before any is used.  CSR entries: g lanes per row
-// into a per-warp row buffer in shared memory (warp-synchronous only).
+// into a per-warp row buffer in shared memory (warp-synchronous only).  The
+// items of a split tile store partial row sums and the last one to arrive
+// adds them, so a launch needs no combine pass.
 // ---------------------------------------------------------------------------
 constexpr int WI_WARPS = 8;
 
@@ -183,6 +185,29 @@ spmv_warp_items_kernel(const LaunchArgs a) {
         if (v1) put(lane + 32, c1 + rows[lane + 32]);
         if (v2) put(lane + 64, c2 + rows[lane + 64]);
         if (v3) put(lane + 96, c3 + rows[lane + 96]);
+    }
+    if (hd.nitem > 1) {
+        // Split tile: the last of its items to arrive adds all partials in
+        // item order and writes y (no combine launch).  Each lane orders its
+        // own partial stores at gpu scope before the warp's arrival; the last
+        // warp's lanes fence again before reading the other items' partials
+        // through L2.
+        __threadfence();
+        __syncwarp();
+        int last = 0;
+        if (lane == 0) last = arrive_acq_rel(io.counters + hd.tile) == hd.nitem - 1;
+        last = __shfl_sync(FULL, last, 0);
+        if (last) {
+            __threadfence();
+            const float *Pp = io.partial + hd.part_base;
+            for (int i = lane; i < h; i += 32) {
+                float sum = 0.f;
+                for (int k = 0; k < hd.nitem; ++k) sum += __ldcg(Pp + (int64_t)k * h + i);
+                io.y[hd.row0 + i] = sum;
+            }
+            __syncwarp();
+            if (lane == 0) io.counters[hd.tile] = 0;  // ready for the next launch
+        }
     }
     if (TIMED) {
         __syncwarp();
