@@ -328,8 +328,12 @@ def run_sable(args):
 
     pk = peaks()
     achieved = B / (statistics.mean(t_learn) * 1e-3) / 1e9
-    traffic = None   # DRAM bytes per launch of the work-item kernel, from the committed ncu summary
-    tf = ROOT / "profiles" / "spmv_items_kernel_spmv_100k.md"
+    # DRAM bytes per launch of the work-item kernel the autotuner picked, from
+    # the committed ncu summary of that kernel on this workload
+    kernel = {"items": "spmv_items_kernel", "warp_items": "spmv_warp_items_kernel",
+              "ring": "batch_kernel"}[learned.config["executor"]]
+    traffic = None
+    tf = ROOT / "profiles" / f"{kernel}_spmv_100k.md"
     if tf.exists():
         hit = re.search(r"traffic_bytes_per_launch:\s*(\d+)", tf.read_text())
         traffic = int(hit.group(1)) if hit else None
@@ -345,7 +349,8 @@ def run_sable(args):
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
-                     "peak_source": pk["source"], "kernel": "spmv_items_kernel (+ split-tile combine) per step"},
+                     "peak_source": pk["source"],
+                     "kernel": kernel + ("" if learned.launches_per_run() == 1 else " + spmv_combine_kernel")},
         "e2e": {"value": round(world * B / e2e_s / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * m.n_cols,
                 "d2h_bytes_per_step": 4 * m.n_rows},
         "gpu_launches": args.steps * learned.launches_per_run(),
