@@ -86,12 +86,60 @@ spmv_items_kernel(const LaunchArgs a) {
 // and the SM keeps as many loads in flight as it has warps.  Dense panel:
 // for h <= 32 a warp step covers floor(32/h) quads (lane = (row, quad
 // offset)), for h > 32 lanes own rows lane, lane+32, ...; four quads per
-// step, their loads issued before any is used.  CSR entries: g lanes per row
-// into a per-warp row buffer in shared memory (warp-synchronous only).  The
+// step, their loads issued before any is used; the x values of the panel
+// columns are gathered once per item into shared memory.  CSR entries: in
+// chunks (warp_csr_chunks) into a per-warp row buffer in shared memory
+// (warp-synchronous only).  The
 // items of a split tile store partial row sums and the last one to arrive
 // adds them, so a launch needs no combine pass.
 // ---------------------------------------------------------------------------
 constexpr int WI_WARPS = 8;
+constexpr int WI_XG = 1024;  // x values of an item's panel columns gathered per warp (floats)
+constexpr int WI_CSR = 256;  // CSR entries per chunk of the per-warp CSR pass (8 per lane)
+
+// CSR entries of a warp's item in chunks of WI_CSR: every lane loads its 8
+// entries of the chunk and then their 8 x values (all independent: two
+// memory round trips per chunk), stores the products in `prod`, and the rows
+// are then summed from shared memory by groups of g lanes (g = 32 / h rounded
+// down to a power of two, at least 1), chunk after chunk, in a fixed order.
+// Adds each row's sum into rows[r].
+__device__ __forceinline__ void warp_csr_chunks(const int *rp, const uint2 *E, int h, int ns, int lane,
+                                                const float *__restrict__ x, float *rows, float *prod) {
+    int g = 32;
+    while (g > 1 && g * h > 32) g >>= 1;
+    const int gpw = 32 / g, sg = lane / g, sl = lane % g;
+    for (int c0 = 0; c0 < ns; c0 += WI_CSR) {
+        const int c1 = min(ns, c0 + WI_CSR);
+        uint2 en[WI_CSR / 32];
+#pragma unroll
+        for (int u = 0; u < WI_CSR / 32; ++u) {
+            const int e = c0 + lane + 32 * u;
+            en[u] = e < c1 ? E[e] : make_uint2(0u, 0u);
+        }
+        float xv[WI_CSR / 32];
+#pragma unroll
+        for (int u = 0; u < WI_CSR / 32; ++u) {
+            const int e = c0 + lane + 32 * u;
+            xv[u] = e < c1 ? __ldg(x + en[u].y) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < WI_CSR / 32; ++u) prod[lane + 32 * u] = __uint_as_float(en[u].x) * xv[u];
+        __syncwarp();
+        for (int r0 = 0; r0 < h; r0 += gpw) {
+            const int r = r0 + sg;
+            int b = 0, e = 0;
+            if (r < h) {
+                b = max(rp[r], c0) - c0;
+                e = min(rp[r + 1], c1) - c0;
+            }
+            float sum = 0.f;
+            for (int i = b + sl; i < e; i += g) sum += prod[i];
+            for (int o = g >> 1; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
+            if (sl == 0 && r < h && e > b) rows[r] += sum;
+        }
+        __syncwarp();
+    }
+}
 
 __device__ __forceinline__ float4 ld_stream(const float4 *p) { return __ldcs(p); }
 
@@ -99,6 +147,8 @@ template <bool TIMED>
 __global__ void __launch_bounds__(WI_WARPS * 32, 4)
 spmv_warp_items_kernel(const LaunchArgs a) {
     __shared__ float s_rows[WI_WARPS][SABLE_MAX_ROW_TILE];  // CSR row sums of each warp's item
+    __shared__ __align__(16) float s_xg[WI_WARPS][WI_XG];     // x of each warp's panel columns
+    __shared__ float s_prod[WI_WARPS][WI_CSR];                // CSR products of one chunk
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int item = blockIdx.x * WI_WARPS + w;
     if (item >= a.n_items) return;  // the whole warp leaves; no CTA barrier follows
@@ -123,11 +173,38 @@ spmv_warp_items_kernel(const LaunchArgs a) {
     const float4 *P = reinterpret_cast<const float4 *>(R + hd.panel_off);
     float *rows = s_rows[w];
     for (int i = lane; i < h; i += 32) rows[i] = 0.f;
+    // x of the panel columns, gathered once for the item: all lanes issue
+    // their column-index and x loads together (GU per lane in flight), so the
+    // quad loop below waits on panel loads only.
+    const bool xg_ok = 4 * nq <= WI_XG;
+    float *xg = s_xg[w];
+    if (xg_ok) {
+        constexpr int GU = 8;
+        const int *xcol = reinterpret_cast<const int *>(xc);
+        for (int base = lane; base < 4 * nq; base += 32 * GU) {
+            float v[GU];
+#pragma unroll
+            for (int u = 0; u < GU; ++u) {
+                const int k = base + 32 * u;
+                v[u] = k < 4 * nq ? __ldg(x + __ldg(xcol + k)) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < GU; ++u) {
+                const int k = base + 32 * u;
+                if (k < 4 * nq) xg[k] = v[u];
+            }
+        }
+    }
     __syncwarp();
+    const float4 *xg4 = reinterpret_cast<const float4 *>(xg);
+    auto xq = [&](int q) { return xg_ok ? xg4[q] : xquad(xc, q, x); };
     if (ns > 0) {
         const int *rp = reinterpret_cast<const int *>(R + hd.rp_off);
         const uint2 *E = reinterpret_cast<const uint2 *>(R + hd.csr_off);
-        csr_rows(rp, E, h, hd.g, 0, ns, lane, rows, [&](int, unsigned col) { return __ldg(x + col); });
+        // short tiles: chunked entries (many lanes per row); tall tiles: a
+        // lane group per row, where a chunk would leave one lane per row
+        if (h <= 16) warp_csr_chunks(rp, E, h, ns, lane, x, rows, s_prod[w]);
+        else csr_rows(rp, E, h, hd.g, 0, ns, lane, rows, [&](int, unsigned col) { return __ldg(x + col); });
     }
     auto put = [&](int i, float v) {
         if (hd.nitem <= 1) io.y[hd.row0 + i] = v;
@@ -141,14 +218,14 @@ spmv_warp_items_kernel(const LaunchArgs a) {
             for (; q + 3 * qpw < nq; q += 4 * qpw) {
                 const float4 p0 = ld_stream(P + q * h + r), p1 = ld_stream(P + (q + qpw) * h + r);
                 const float4 p2 = ld_stream(P + (q + 2 * qpw) * h + r), p3 = ld_stream(P + (q + 3 * qpw) * h + r);
-                const float4 x0 = xquad(xc, q, x), x1 = xquad(xc, q + qpw, x);
-                const float4 x2 = xquad(xc, q + 2 * qpw, x), x3 = xquad(xc, q + 3 * qpw, x);
+                const float4 x0 = xq(q), x1 = xq(q + qpw);
+                const float4 x2 = xq(q + 2 * qpw), x3 = xq(q + 3 * qpw);
                 a0 = dot4(p0, x0, a0);
                 a1 = dot4(p1, x1, a1);
                 a0 = dot4(p2, x2, a0);
                 a1 = dot4(p3, x3, a1);
             }
-            for (; q < nq; q += qpw) a0 = dot4(ld_stream(P + q * h + r), xquad(xc, q, x), a0);
+            for (; q < nq; q += qpw) a0 = dot4(ld_stream(P + q * h + r), xq(q), a0);
         }
         const float v = a0 + a1;
         float tot = 0.f;
@@ -160,7 +237,7 @@ spmv_warp_items_kernel(const LaunchArgs a) {
         float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
         int q = 0;
         for (; q + 1 < nq; q += 2) {
-            const float4 xa = xquad(xc, q, x), xb = xquad(xc, q + 1, x);
+            const float4 xa = xq(q), xb = xq(q + 1);
             const float4 *Pa = P + q * h + lane, *Pb = Pa + h;
             const float4 pa0 = ld_stream(Pa), pb0 = ld_stream(Pb);
             float4 pa1 = make_float4(0.f, 0.f, 0.f, 0.f), pb1 = pa1, pa2 = pa1, pb2 = pa1, pa3 = pa1, pb3 = pa1;
@@ -173,7 +250,7 @@ spmv_warp_items_kernel(const LaunchArgs a) {
             c3 = dot4(pb3, xb, dot4(pa3, xa, c3));
         }
         if (q < nq) {
-            const float4 xa = xquad(xc, q, x);
+            const float4 xa = xq(q);
             const float4 *Pa = P + q * h + lane;
             c0 = dot4(ld_stream(Pa), xa, c0);
             if (v1) c1 = dot4(ld_stream(Pa + 32), xa, c1);
