@@ -58,7 +58,38 @@
 
 namespace {
 
-constexpr int KSTEP = 16;  // panel columns per staging step
+constexpr int KSTEP = 16;   // panel columns per staging step
+constexpr int KSTAGES = 4;  // K steps in flight (cp.async pipeline depth)
+
+// 16-byte asynchronous copy global -> shared; when !valid, nothing is read
+// (src-size 0) and the 16 bytes are zero-filled.
+__device__ __forceinline__ void cp16z(void *dst, const void *src, bool valid) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;"
+                 :: "r"(smem_addr(dst)), "l"(src), "r"(valid ? 16 : 0) : "memory");
+}
+
+// Starts the copies of K step k0 into one stage: the KSTEP X rows of the
+// step's panel columns (NT/4 float4 each, through colmap) and its KSTEP/4
+// panel quads of every row.  Out-of-range parts are zero-filled.  The caller
+// commits the group.
+template <int NT>
+__device__ __forceinline__ void stage_kstep(float4 *Bs, float4 *As, int k0, int ncol, const int *colmap,
+                                            const float *X, int64_t ldx, int N, int n0, const float4 *P, int h,
+                                            int nq) {
+    constexpr int CQ = NT / 4;
+    for (int t = threadIdx.x; t < KSTEP * CQ; t += SABLE_THREADS) {
+        const int kk = t / CQ, q = t - kk * CQ, k = k0 + kk, n = n0 + 4 * q;
+        const bool ok = k < ncol && n < N;
+        const float *src = ok ? X + (int64_t)__ldg(colmap + k) * ldx + n : X;
+        cp16z(&Bs[t], src, ok);
+    }
+    const int qbase = k0 >> 2;
+    for (int t = threadIdx.x; t < (KSTEP / 4) * h; t += SABLE_THREADS) {
+        const int qq = t / h, i = t - qq * h, q = qbase + qq;
+        const bool ok = q < nq;
+        cp16z(&As[qq * SABLE_MAX_ROW_TILE + i], ok ? P + (int64_t)q * h + i : P, ok);
+    }
+}
 
 template <int NT>
 struct SpmmSmem {
@@ -67,9 +98,12 @@ struct SpmmSmem {
     static constexpr int BS = KSTEP * CQ * 16;                     // staged X rows
     static constexpr int AS = (KSTEP / 4) * SABLE_MAX_ROW_TILE * 16;  // staged quads
     static constexpr int RST = (SABLE_MAX_ROW_TILE + 8) * 4;
-    static constexpr int OFF_BS = YS;
-    static constexpr int OFF_AS = OFF_BS + BS;
-    static constexpr int OFF_RST = OFF_AS + AS;
+    // The K-loop stages share the space of the Y tile, which is only used
+    // after the loop.
+    static constexpr int OFF_BS = 0;                              // KSTAGES stages of X rows
+    static constexpr int OFF_AS = OFF_BS + KSTAGES * BS;          // KSTAGES stages of quads
+    static constexpr int LOOP = OFF_AS + KSTAGES * AS;
+    static constexpr int OFF_RST = (YS > LOOP ? YS : LOOP);
     static constexpr int TOTAL = OFF_RST + RST;
 };
 
@@ -102,34 +136,37 @@ __device__ __forceinline__ void spmm_fp32_item(const unsigned char *R, const Mat
 #pragma unroll
     for (int m = 0; m < RM; ++m) acc[m] = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 *__restrict__ P = reinterpret_cast<const float4 *>(R + c.panel_off);
-    for (int k0 = 0; k0 < ncol; k0 += KSTEP) {
-        for (int t = tid; t < KSTEP * CQ; t += SABLE_THREADS) {
-            const int kk = t / CQ, q = t - kk * CQ, k = k0 + kk, n = n0 + 4 * q;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (k < ncol && n < a.N) {
-                const int col = __ldg(colmap + k);
-                v = __ldg(reinterpret_cast<const float4 *>(X + (int64_t)col * a.ldx + n));
-            }
-            Bs[t] = v;
-        }
-        const int qbase = k0 >> 2;
-        for (int t = tid; t < (KSTEP / 4) * h; t += SABLE_THREADS) {
-            const int qq = t / h, i = t - qq * h, q = qbase + qq;
-            As[qq * SABLE_MAX_ROW_TILE + i] =
-                q < nq ? __ldcs(P + (int64_t)q * h + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
+    // KSTAGES-deep pipeline: the copies of steps k+1 .. k+KSTAGES-1 are in
+    // flight while step k is computed (one commit group per step, empty past
+    // the end, so wait_group KSTAGES-1 always means "step k has landed")
+    for (int st = 0; st < KSTAGES - 1; ++st) {
+        if (st * KSTEP < ncol)
+            stage_kstep<NT>(Bs + st * (KSTEP * CQ), As + st * ((KSTEP / 4) * SABLE_MAX_ROW_TILE), st * KSTEP, ncol,
+                            colmap, X, a.ldx, a.N, n0, P, h, nq);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    int buf = 0;
+    for (int k0 = 0; k0 < ncol; k0 += KSTEP, buf = (buf + 1) % KSTAGES) {
+        const int nk = k0 + (KSTAGES - 1) * KSTEP, nb = (buf + KSTAGES - 1) % KSTAGES;
+        if (nk < ncol)
+            stage_kstep<NT>(Bs + nb * (KSTEP * CQ), As + nb * ((KSTEP / 4) * SABLE_MAX_ROW_TILE), nk, ncol, colmap, X,
+                            a.ldx, a.N, n0, P, h, nq);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group %0;" :: "n"(KSTAGES - 1) : "memory");
         __syncthreads();
+        const float4 *Bsb = Bs + buf * (KSTEP * CQ);
+        const float4 *Asb = As + buf * ((KSTEP / 4) * SABLE_MAX_ROW_TILE);
 #pragma unroll
         for (int qq = 0; qq < KSTEP / 4; ++qq) {
-            const float4 b0 = Bs[(4 * qq + 0) * CQ + cq];
-            const float4 b1 = Bs[(4 * qq + 1) * CQ + cq];
-            const float4 b2 = Bs[(4 * qq + 2) * CQ + cq];
-            const float4 b3 = Bs[(4 * qq + 3) * CQ + cq];
+            const float4 b0 = Bsb[(4 * qq + 0) * CQ + cq];
+            const float4 b1 = Bsb[(4 * qq + 1) * CQ + cq];
+            const float4 b2 = Bsb[(4 * qq + 2) * CQ + cq];
+            const float4 b3 = Bsb[(4 * qq + 3) * CQ + cq];
 #pragma unroll
             for (int m = 0; m < RM; ++m) {
                 const int i = rg + NRG * m;
                 if (i < h) {
-                    const float4 av = As[qq * SABLE_MAX_ROW_TILE + i];
+                    const float4 av = Asb[qq * SABLE_MAX_ROW_TILE + i];
                     acc[m] = fma4(av.x, b0, acc[m]);
                     acc[m] = fma4(av.y, b1, acc[m]);
                     acc[m] = fma4(av.z, b2, acc[m]);
@@ -139,6 +176,7 @@ __device__ __forceinline__ void spmm_fp32_item(const unsigned char *R, const Mat
         }
         __syncthreads();
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");  // the Y tile reuses the stage space
 #pragma unroll
     for (int m = 0; m < RM; ++m) {
         const int i = rg + NRG * m;
@@ -258,9 +296,12 @@ struct TcSmem {
     static constexpr int BS = KSTEP * NT * 4;                            // staged X rows (FP32)
     static constexpr int AS = (KSTEP / 4) * SABLE_MAX_ROW_TILE * 16;     // staged quads
     static constexpr int RST = (SABLE_MAX_ROW_TILE + 8) * 4;
-    static constexpr int OFF_BS = YS;
-    static constexpr int OFF_AS = OFF_BS + BS;
-    static constexpr int OFF_RST = OFF_AS + AS;
+    // The K-loop stages share the space of the Y tile, which is only used
+    // after the loop.
+    static constexpr int OFF_BS = 0;                              // KSTAGES stages of X rows
+    static constexpr int OFF_AS = OFF_BS + KSTAGES * BS;          // KSTAGES stages of quads
+    static constexpr int LOOP = OFF_AS + KSTAGES * AS;
+    static constexpr int OFF_RST = (YS > LOOP ? YS : LOOP);
     static constexpr int TOTAL = OFF_RST + RST;
 };
 
@@ -270,7 +311,8 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
     using L = TcSmem<NT>;
     constexpr int CQ = L::CQ;
     constexpr int NTILES = NT / 8;                        // 8-column MMA tiles of the slice
-    constexpr int WN = NTILES < 8 ? NTILES : 8;           // warps along N
+    constexpr int WN = NTILES < 4 ? NTILES : 4;           // warps along N (4 x 2 grid: each A fragment is
+                                                          // split by 4 warps, not 8)
     constexpr int WM = 8 / WN;                            // warps along M
     constexpr int NPW = (NTILES + WN - 1) / WN;           // N-tiles per warp
     constexpr int MPW = (SABLE_MAX_ROW_TILE / 16 + WM - 1) / WM;  // M-tiles per warp (max)
@@ -302,21 +344,25 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
 #pragma unroll
             for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
 
-    for (int k0 = 0; k0 < ncol; k0 += KSTEP) {
-        // stage 16 X rows (FP32) and 4 panel quads
-        for (int e = tid; e < KSTEP * CQ; e += SABLE_THREADS) {
-            const int kk = e / CQ, q = e - kk * CQ, k = k0 + kk, n = n0 + 4 * q;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (k < ncol && n < a.N) v = __ldg(reinterpret_cast<const float4 *>(X + (int64_t)__ldg(colmap + k) * a.ldx + n));
-            reinterpret_cast<float4 *>(Bs)[e] = v;
-        }
-        const int qbase = k0 >> 2;
-        for (int e = tid; e < (KSTEP / 4) * h; e += SABLE_THREADS) {
-            const int qq = e / h, i = e - qq * h, q = qbase + qq;
-            As[qq * SABLE_MAX_ROW_TILE + i] = q < nq ? __ldcs(P + (int64_t)q * h + i) : make_float4(0.f, 0.f, 0.f, 0.f);
-        }
+    // KSTAGES-deep pipeline, as in spmm_fp32_item
+    float4 *Bs4 = reinterpret_cast<float4 *>(Bs);
+    for (int st = 0; st < KSTAGES - 1; ++st) {
+        if (st * KSTEP < ncol)
+            stage_kstep<NT>(Bs4 + st * (KSTEP * CQ), As + st * ((KSTEP / 4) * SABLE_MAX_ROW_TILE), st * KSTEP, ncol,
+                            colmap, X, a.ldx, a.N, n0, P, h, nq);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    int buf = 0;
+    for (int k0 = 0; k0 < ncol; k0 += KSTEP, buf = (buf + 1) % KSTAGES) {
+        const int nk = k0 + (KSTAGES - 1) * KSTEP, nb = (buf + KSTAGES - 1) % KSTAGES;
+        if (nk < ncol)
+            stage_kstep<NT>(Bs4 + nb * (KSTEP * CQ), As + nb * ((KSTEP / 4) * SABLE_MAX_ROW_TILE), nk, ncol, colmap, X,
+                            a.ldx, a.N, n0, P, h, nq);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group %0;" :: "n"(KSTAGES - 1) : "memory");
         __syncthreads();
-        const float *Af = reinterpret_cast<const float *>(As);
+        const float *Bsb = Bs + buf * (KSTEP * NT);
+        const float *Af = reinterpret_cast<const float *>(As + buf * ((KSTEP / 4) * SABLE_MAX_ROW_TILE));
         // B fragments of this warp's N-tiles: bt[j][term][register]
         uint32_t bt[NPW][TERMS][2];
 #pragma unroll
@@ -325,10 +371,10 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
             const int col = nt * 8 + g;
             float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
             if (nt < NTILES) {
-                v0 = Bs[(2 * t) * NT + col];
-                v1 = Bs[(2 * t + 1) * NT + col];
-                v2 = Bs[(2 * t + 8) * NT + col];
-                v3 = Bs[(2 * t + 9) * NT + col];
+                v0 = Bsb[(2 * t) * NT + col];
+                v1 = Bsb[(2 * t + 1) * NT + col];
+                v2 = Bsb[(2 * t + 8) * NT + col];
+                v3 = Bsb[(2 * t + 9) * NT + col];
             }
             uint32_t s0[TERMS], s1[TERMS];
             split<TERMS>(v0, v1, s0);
@@ -364,23 +410,27 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
                 at[k][2] = s01[k];
                 at[k][3] = s11[k];
             }
+            // products in the order (a-term, b-term), smallest terms first; the
+            // N-tile loop inside, so consecutive MMAs go to independent
+            // accumulators
+            constexpr int NPROD = TERMS == 3 ? 6 : 3;
+            constexpr int PA[6] = {1, 0, 2, 0, 1, 0}, PB[6] = {1, 2, 0, 1, 0, 0};
+            constexpr int QA[3] = {0, 1, 0}, QB[3] = {1, 0, 0};
 #pragma unroll
-            for (int j = 0; j < NPW; ++j) {
-                if (wn + j * WN >= NTILES) continue;
-                // smallest terms first
-                if (TERMS == 3) {
-                    mma_bf16(acc[i][j], at[1], bt[j][1]);
-                    mma_bf16(acc[i][j], at[0], bt[j][TERMS - 1]);
-                    mma_bf16(acc[i][j], at[TERMS - 1], bt[j][0]);
+            for (int pr = 0; pr < NPROD; ++pr) {
+                const int ta = TERMS == 3 ? PA[pr] : QA[pr], tb = TERMS == 3 ? PB[pr] : QB[pr];
+#pragma unroll
+                for (int j = 0; j < NPW; ++j) {
+                    if (wn + j * WN >= NTILES) continue;
+                    mma_bf16(acc[i][j], at[ta], bt[j][tb]);
                 }
-                mma_bf16(acc[i][j], at[0], bt[j][1]);
-                mma_bf16(acc[i][j], at[1], bt[j][0]);
-                mma_bf16(acc[i][j], at[0], bt[j][0]);
             }
         }
         __syncthreads();
     }
-    // accumulators -> Y tile (rows >= h are not stored; all rows < h are written)
+    // accumulators -> Y tile (rows >= h are not stored; all rows < h are written);
+    // the Y tile reuses the stage space
+    asm volatile("cp.async.wait_all;" ::: "memory");
     for (int e = tid; e < h * CQ; e += SABLE_THREADS) ys4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
 #pragma unroll
