@@ -35,6 +35,17 @@ from . import fileio
 from .convert import Compressed, block_nnz, block_table, compress
 from .plan import Plan
 
+# Launch shapes the entry points use unless plan options say otherwise: the
+# fastest shapes measured on large matrices (one warp per 32 KB work item over
+# 8-row tiles for SpMV; one CTA per work item with separate dense and CSR
+# items for SpMM).  sable_gb300.autotune picks per matrix.
+SPMV_SHAPE = {"schedule": "warp_items", "row_tile": 8, "chunk_bytes": 32768}
+SPMM_SHAPE = {"split_layout": "separate"}
+
+
+def _with(defaults: dict, opts: dict) -> dict:
+    return {**defaults, **opts}
+
 PLANS: dict = {}
 
 
@@ -88,7 +99,7 @@ def gen_single_threaded_spmv(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, ubl
                              dir_name, filename, vbr_dir, bench: int = 5, **plan_opts) -> int:
     t1 = time.time_ns() // 1_000_000
     comp = _compressed_from_vbrc(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, ublocks, indptr, indices, csr_val)
-    plan = Plan(comp, **plan_opts)
+    plan = Plan(comp, **_with(SPMV_SHAPE, plan_opts))
     _register(dir_name, filename, PlanRecord(plan, "spmv", comp.n_rows, comp.n_cols, bench,
                                              {"vbr_dir": os.path.abspath(vbr_dir), "threads": 1}))
     return time.time_ns() // 1_000_000 - t1
@@ -158,7 +169,7 @@ def gen_single_threaded_spmm(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, den
                              filename: str, vbr_dir: str, spmm_tc="split3", **plan_opts) -> PlanRecord:
     bt, dense = _density_mask(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density)
     comp = compress(np.asarray(val, dtype=np.float32), rpntr, cpntr, indx, bindx, bpntrb, bpntre, dense, bt=bt)
-    plan = Plan(comp, spmm_tc=spmm_tc, **plan_opts)
+    plan = Plan(comp, spmm_tc=spmm_tc, **_with(SPMM_SHAPE, plan_opts))
     rec = PlanRecord(plan, "spmm", comp.n_rows, comp.n_cols, 1,
                      {"vbr_dir": os.path.abspath(vbr_dir), "density": density, "threads": 1, "spmm_tc": plan.spmm_tc})
     _register(dir_name, filename, rec)
@@ -209,7 +220,7 @@ def vbr_spmv_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: i
     t1 = time.time_ns() // 1_000
     bt, dense = _density_mask(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density, integer_rule=True)
     comp = compress(np.asarray(val, dtype=np.float32), rpntr, cpntr, indx, bindx, bpntrb, bpntre, dense, bt=bt)
-    _register(dir_name, filename, PlanRecord(Plan(comp, **plan_opts), "spmv", comp.n_rows, comp.n_cols, 0,
+    _register(dir_name, filename, PlanRecord(Plan(comp, **_with(SPMV_SHAPE, plan_opts)), "spmv", comp.n_rows, comp.n_cols, 0,
                                              {"density": density}))
     return time.time_ns() // 1_000 - t1
 
@@ -220,6 +231,7 @@ def vbr_spmm_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: i
     t1 = time.time_ns() // 1_000
     bt, dense = _density_mask(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density, integer_rule=True)
     comp = compress(np.asarray(val, dtype=np.float32), rpntr, cpntr, indx, bindx, bpntrb, bpntre, dense, bt=bt)
-    _register(dir_name, filename, PlanRecord(Plan(comp, spmm_tc=spmm_tc, **plan_opts), "spmm", comp.n_rows,
+    _register(dir_name, filename, PlanRecord(Plan(comp, spmm_tc=spmm_tc, **_with(SPMM_SHAPE, plan_opts)), "spmm",
+                                             comp.n_rows,
                                              comp.n_cols, 0, {"density": density}))
     return time.time_ns() // 1_000 - t1
