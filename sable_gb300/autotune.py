@@ -34,7 +34,7 @@ SPMV_CANDIDATES = [
     {"executor": "ring", "row_tile": 128, "chunk_bytes": cb, "stages": s} for cb in (16384, 32768) for s in (2, 3)
 ]
 SPMM_CANDIDATES = [
-    {"executor": "items", "row_tile": rt, "chunk_bytes": cb} for rt in (128, 64) for cb in (16384, 32768)
+    {"executor": "items", "row_tile": rt, "chunk_bytes": cb} for rt in (128, 64) for cb in (16384, 32768, 49152, 65536)
 ] + [{"executor": "ring", "row_tile": 128, "chunk_bytes": 32768, "stages": 2}]
 
 _cache: dict[str, dict] = {}
