@@ -322,6 +322,8 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     for (int i = 0; i < n_plans; ++i) {
         if (!plans[i]) return fail(SABLE_ERR_ARG, "plan %d is null", i);
         if (plans[i]->device != plans[0]->device) return fail(SABLE_ERR_ARG, "plans on different devices");
+        if (plans[i]->compact)
+            return fail(SABLE_ERR_UNSUPPORTED, "plan %d: a plan of the per-warp SpMV executor (schedule 2) is not batched", i);
         if (widths[i] < 1 || (widths[i] > 1 && (widths[i] & 3)))
             return fail(SABLE_ERR_UNSUPPORTED, "width %d of matrix %d: 1, or a multiple of 4", widths[i], i);
     }

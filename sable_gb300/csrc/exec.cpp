@@ -38,6 +38,7 @@ int plan_upload(sable_plan *p, const Layout &L) {
     p->max_item_bytes = std::max(L.max_item_bytes, 64);
     p->max_xg_floats = std::max(L.max_xg_floats, 4);
     p->records_bytes = (int64_t)L.records.size();
+    p->compact = L.compact;
     int64_t bytes = 0;
     int rc;
     // item table, largest first (one CTA per item launches and the timed form)
@@ -183,6 +184,7 @@ static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_
         return fail(SABLE_ERR_UNSUPPORTED, "SpMM needs N %% 4 == 0 and ld >= N, ld %% 4 == 0 (N=%d ldx=%lld ldy=%lld)", N,
                     (long long)ldx, (long long)ldy);
     if (((uintptr_t)X & 15) || ((uintptr_t)Y & 15)) return fail(SABLE_ERR_UNSUPPORTED, "SpMM operands must be 16-byte aligned");
+    if (p->compact) return fail(SABLE_ERR_UNSUPPORTED, "a plan of the per-warp SpMV executor (schedule 2) runs SpMV only");
     int rc = set_device(p->device);
     if (rc) return rc;
     const int nt = pick_nt(N);

@@ -150,7 +150,44 @@ static int collect_dense(const sable_vbrc_desc *d, std::vector<std::vector<Dense
 // ---------------------------------------------------------------------------
 static inline int64_t pad16(int64_t b) { return (b + 15) & ~(int64_t)15; }
 
-int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int split_layout, Layout &L) {
+namespace {
+struct Run { int32_t col0, len; };  // window run: first x column (-1: zeros), positions
+
+// Window runs of one compact item: the panel columns xcol[4 q0, 4 q1) (-1 for
+// padding), then the sorted distinct columns of CSR entries [e0, e1) of
+// `indices`, runs closer than SABLE_CW_GAP merged.  Returns the window length;
+// n_dense_runs = runs of the panel part.
+int64_t compact_window(const int32_t *xcol, int64_t q0, int64_t q1, const int32_t *indices, int64_t e0, int64_t e1,
+                       std::vector<Run> &runs, size_t &n_dense_runs, std::vector<int32_t> &scratch) {
+    runs.clear();
+    for (int64_t p = 4 * q0; p < 4 * q1; ++p) {
+        const int32_t c = xcol[p];
+        if (!runs.empty()) {
+            Run &r = runs.back();
+            if ((c < 0 && r.col0 < 0) || (c >= 0 && r.col0 >= 0 && r.col0 + r.len == c)) { ++r.len; continue; }
+        }
+        runs.push_back({c < 0 ? -1 : c, 1});
+    }
+    n_dense_runs = runs.size();
+    int64_t nw = 4 * (q1 - q0);
+    if (e1 > e0) {
+        scratch.assign(indices + e0, indices + e1);
+        std::sort(scratch.begin(), scratch.end());
+        scratch.erase(std::unique(scratch.begin(), scratch.end()), scratch.end());
+        for (int32_t c : scratch) {
+            if (runs.size() > n_dense_runs) {
+                Run &r = runs.back();
+                if (c - (r.col0 + r.len) < SABLE_CW_GAP) { r.len = c - r.col0 + 1; continue; }
+            }
+            runs.push_back({c, 1});
+        }
+        for (size_t k = n_dense_runs; k < runs.size(); ++k) nw += runs[k].len;
+    }
+    return nw;
+}
+}  // namespace
+
+int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int split_layout, Layout &L, bool compact) {
     std::vector<std::vector<DenseBlock>> rows;
     int rc = collect_dense(d, rows);
     if (rc) return rc;
@@ -223,6 +260,151 @@ int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int spl
         L.max_xg_floats = std::max<int>(L.max_xg_floats, 4 * nq + ns);
     };
 
+    // Compact record of quads [q0, q1) and tile CSR entries [s0, s1) (global
+    // entry k0 + s); the caller has checked that its window fits.
+    std::vector<Run> runs;
+    std::vector<int32_t> scratch;
+    auto emit_compact = [&](int32_t row0, int32_t h, int64_t q0, int64_t q1, int64_t s0, int64_t s1, int64_t k0,
+                            int32_t tile, int32_t kidx, int32_t nitem, int64_t part_base) -> int {
+        size_t nd_runs = 0;
+        const int64_t nw = compact_window(xcol.data(), q0, q1, d->indices, k0 + s0, k0 + s1, runs, nd_runs, scratch);
+        if (nw > SABLE_CW_MAX) return fail(SABLE_ERR_INVALID, "layout: compact window %lld", (long long)nw);
+        const int32_t nq = (int32_t)(q1 - q0), ns = (int32_t)(s1 - s0), nrun = (int32_t)runs.size();
+        CompactHeader hd;
+        memset(&hd, 0, sizeof hd);
+        hd.row0 = row0;
+        hd.h = h;
+        hd.nq = nq;
+        hd.ns = ns;
+        int64_t off = sizeof(CompactHeader);
+        hd.runs_off = (int32_t)off;
+        off += pad16(8 * (int64_t)nrun);
+        hd.panel_off = (int32_t)off;
+        off += 16 * (int64_t)nq * h;
+        hd.rp_off = (int32_t)off;
+        hd.val_off = (int32_t)off;
+        off += 32 * (((int64_t)ns + 7) / 8);  // whole groups of 8 entries
+        hd.meta_off = (int32_t)off;
+        off += 16 * (((int64_t)ns + 7) / 8);
+        hd.bytes = (int32_t)off;
+        hd.tile = tile;
+        hd.kidx = kidx;
+        hd.nitem = nitem;
+        hd.part_base = part_base;
+        hd.nrun = (int16_t)nrun;
+        hd.nw = (int16_t)nw;
+        const int64_t base = (int64_t)L.records.size();
+        L.records.resize(base + hd.bytes, 0);
+        unsigned char *R = L.records.data() + base;
+        memcpy(R, &hd, sizeof hd);
+        memcpy(R + hd.runs_off, runs.data(), 8 * (size_t)nrun);
+        memcpy(R + hd.panel_off, panel.data() + q0 * h, 16 * (size_t)nq * h);
+        if (ns > 0) {
+            memcpy(R + hd.val_off, d->csr_val + k0 + s0, 4 * (size_t)ns);
+            // window position of each entry's column (its run's first position
+            // + offset) and the entry's tile row
+            std::vector<int64_t> start(nrun + 1 - nd_runs);
+            start[0] = 4 * (int64_t)nq;
+            for (size_t r = nd_runs; r < runs.size(); ++r) start[r - nd_runs + 1] = start[r - nd_runs] + runs[r].len;
+            uint16_t *meta = reinterpret_cast<uint16_t *>(R + hd.meta_off);
+            int32_t row = 0;
+            for (int64_t k = 0; k < ns; ++k) {
+                while (tp[row + 1] <= s0 + k) ++row;
+                const int32_t c = d->indices[k0 + s0 + k];
+                // last CSR run whose first column is <= c
+                size_t lo = nd_runs, hi = runs.size();
+                while (hi - lo > 1) {
+                    const size_t mid = (lo + hi) / 2;
+                    if (runs[mid].col0 <= c) lo = mid;
+                    else hi = mid;
+                }
+                meta[k] = (uint16_t)((start[lo - nd_runs] + (c - runs[lo].col0)) | (row << 10));
+            }
+        }
+        ItemRef ref;
+        ref.off = base;
+        ref.bytes = hd.bytes;
+        ref.cost = hd.bytes;
+        L.items.push_back(ref);
+        L.item_tile.push_back(tile_id);
+        L.max_item_bytes = std::max<int>(L.max_item_bytes, hd.bytes);
+        L.max_xg_floats = std::max<int>(L.max_xg_floats, (int)nw);
+        return SABLE_OK;
+    };
+    // Window length of quads [q0, q1) and CSR entries [s0, s1) of the tile.
+    auto window_of = [&](int64_t q0, int64_t q1, int64_t s0, int64_t s1, int64_t k0) {
+        size_t nd_runs = 0;
+        return compact_window(xcol.data(), q0, q1, d->indices, k0 + s0, k0 + s1, runs, nd_runs, scratch);
+    };
+
+    // Compact items of one tile: a single item when the tile's record fits
+    // item_bytes (+25 %) and its window fits; otherwise a split tile (mixed
+    // layout: equal shares of quads and entries per item; separate layout:
+    // dense items, then CSR items) whose item count grows until every item's
+    // window fits.
+    auto cut_compact = [&](int32_t row0, int32_t h, int64_t nq, int64_t ns, int64_t k0) -> int {
+        const int64_t hdr = sizeof(CompactHeader);
+        {
+            const int64_t nw = window_of(0, nq, 0, ns, k0);
+            const int64_t bytes = hdr + pad16(8 * (int64_t)runs.size()) + 16 * nq * h + 48 * ((ns + 7) / 8);
+            if (nw <= SABLE_CW_MAX && bytes <= item_bytes + item_bytes / 4)
+                return emit_compact(row0, h, 0, nq, 0, ns, k0, -1, 0, 1, 0);
+        }
+        const int64_t avail = std::max<int64_t>(1024, item_bytes - hdr - 128);
+        auto grow = [](int64_t n) { return n + std::max<int64_t>(1, n / 4); };
+        int64_t nd = 0, nsp = 0, nitem;
+        if (split_layout == 0) {
+            nitem = std::max<int64_t>(2, (16 * nq * h + 6 * ns + avail - 1) / avail);
+            for (;;) {
+                bool ok = true;
+                for (int64_t k = 0; k < nitem && ok; ++k)
+                    ok = window_of(nq * k / nitem, nq * (k + 1) / nitem, ns * k / nitem, ns * (k + 1) / nitem, k0) <=
+                         SABLE_CW_MAX;
+                if (ok) break;
+                nitem = grow(nitem);
+            }
+        } else {
+            if (nq > 0) nd = std::max((16 * nq * h + avail - 1) / avail, (4 * nq + SABLE_CW_MAX - 1) / SABLE_CW_MAX);
+            if (ns > 0) {
+                nsp = (6 * ns + avail - 1) / avail;
+                for (;;) {
+                    bool ok = true;
+                    for (int64_t k = 0; k < nsp && ok; ++k)
+                        ok = window_of(0, 0, ns * k / nsp, ns * (k + 1) / nsp, k0) <= SABLE_CW_MAX;
+                    if (ok) break;
+                    nsp = grow(nsp);
+                }
+            }
+            nitem = std::max<int64_t>(2, nd + nsp);
+            if (nd + nsp < 2) nd = nitem - nsp;  // one oversized part: cut its dense quads in two
+        }
+        if (nitem > INT32_MAX / 2) return fail(SABLE_ERR_UNSUPPORTED, "tile at row %d needs %lld items", row0, (long long)nitem);
+        const int32_t sid = split_tiles++;
+        const int64_t pbase = part_floats;
+        part_floats += nitem * h;
+        SplitTile st;
+        st.part_base = pbase;
+        st.row0 = row0;
+        st.h = h;
+        st.nitem = (int32_t)nitem;
+        st.mat = 0;
+        L.splits.push_back(st);
+        int rc2 = SABLE_OK;
+        if (split_layout == 0) {
+            for (int64_t k = 0; k < nitem && !rc2; ++k)
+                rc2 = emit_compact(row0, h, nq * k / nitem, nq * (k + 1) / nitem, ns * k / nitem, ns * (k + 1) / nitem, k0,
+                                   sid, (int32_t)k, (int32_t)nitem, pbase);
+        } else {
+            int32_t kidx = 0;
+            for (int64_t k = 0; k < nd && !rc2; ++k)
+                rc2 = emit_compact(row0, h, nq * k / nd, nq * (k + 1) / nd, 0, 0, k0, sid, kidx++, (int32_t)nitem, pbase);
+            for (int64_t k = 0; k < nsp && !rc2; ++k)
+                rc2 = emit_compact(row0, h, 0, 0, ns * k / nsp, ns * (k + 1) / nsp, k0, sid, kidx++, (int32_t)nitem, pbase);
+        }
+        return rc2;
+    };
+
+    if (compact) row_tile = std::min(row_tile, SABLE_CW_MAX_ROWS);
     for (int32_t a = 0; a < d->n_block_rows; ++a) {
         const int32_t r0 = d->rpntr[a], hb = d->rpntr[a + 1] - r0;
         const int32_t nt = (hb + row_tile - 1) / row_tile;
@@ -234,7 +416,7 @@ int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int spl
             const int32_t h = hi - lo, row0 = r0 + lo;
             // tile panel and its x columns
             panel.assign((size_t)(nq * h), make_float4(0.f, 0.f, 0.f, 0.f));
-            xcol.assign((size_t)(4 * nq), 0);
+            xcol.assign((size_t)(4 * nq), compact ? -1 : 0);
             float *P = reinterpret_cast<float *>(panel.data());
             int32_t pc = 0;
             for (const DenseBlock &db : rows[a]) {
@@ -259,6 +441,11 @@ int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int spl
                 for (int32_t i = 0; i <= h; ++i) tp[i] = d->indptr[row0 + i] - k0;
             }
             L.sparse_nnz += ns;
+            if (compact) {
+                rc = cut_compact(row0, h, nq, ns, k0);
+                if (rc) return rc;
+                continue;
+            }
             // cut into items
             const int64_t hdr = sizeof(ItemHeader);
             const int64_t total = hdr + 16 * nq + 16 * nq * h + (ns ? pad16(4 * ((int64_t)h + 1)) + pad16(8 * ns) : 0);
@@ -311,7 +498,8 @@ int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int spl
     L.n_tiles = tile_id;
     L.n_partial = part_floats;
     L.n_split_tiles = split_tiles;
-    return check_layout(L);
+    L.compact = compact;
+    return compact ? check_compact_layout(L) : check_layout(L);
 }
 
 // Every index a kernel will follow, checked on the host before upload.
@@ -345,6 +533,52 @@ int check_layout(const Layout &L) {
                 if ((int64_t)E[i].y >= L.n_cols) return fail(SABLE_ERR_INVALID, "layout: item %zu CSR column", k);
         }
         if (hd.g != 4 && hd.g != 8 && hd.g != 16 && hd.g != 32) return fail(SABLE_ERR_INVALID, "layout: item %zu lane group", k);
+        if (hd.nitem < 1 || hd.kidx < 0 || hd.kidx >= hd.nitem) return fail(SABLE_ERR_INVALID, "layout: item %zu numbering", k);
+        if (hd.nitem > 1 && (hd.tile < 0 || hd.tile >= L.n_split_tiles || hd.part_base < 0 ||
+                             hd.part_base + (int64_t)hd.nitem * hd.h > L.n_partial))
+            return fail(SABLE_ERR_INVALID, "layout: item %zu split-tile scratch out of bounds", k);
+    }
+    return SABLE_OK;
+}
+
+// Compact records: every index the per-warp kernel follows, checked on the
+// host before upload (runs, window positions, row pointers, split scratch).
+int check_compact_layout(const Layout &L) {
+    const int64_t nrec = (int64_t)L.records.size();
+    for (size_t k = 0; k < L.items.size(); ++k) {
+        const ItemRef &r = L.items[k];
+        if (r.off < 0 || (r.off & 15) || r.bytes < (int)sizeof(CompactHeader) || (r.bytes & 15) ||
+            r.off + r.bytes > nrec || r.bytes > SABLE_MAX_ITEM_BYTES)
+            return fail(SABLE_ERR_INVALID, "layout: item %zu record range", k);
+        CompactHeader hd;
+        memcpy(&hd, L.records.data() + r.off, sizeof hd);
+        if (hd.bytes != r.bytes) return fail(SABLE_ERR_INVALID, "layout: item %zu size mismatch", k);
+        if (hd.h < 1 || hd.h > SABLE_MAX_ROW_TILE || hd.row0 < 0 || hd.row0 + hd.h > L.n_rows)
+            return fail(SABLE_ERR_INVALID, "layout: item %zu rows out of range", k);
+        const int64_t nq = hd.nq, ns = hd.ns, nrun = hd.nrun, nw = hd.nw;
+        if (hd.h > SABLE_CW_MAX_ROWS) return fail(SABLE_ERR_INVALID, "layout: item %zu compact tile height", k);
+        if (nq < 0 || ns < 0 || nrun < 0 || nw < 4 * nq || nw > SABLE_CW_MAX || hd.runs_off != (int)sizeof(CompactHeader) ||
+            hd.panel_off != hd.runs_off + pad16(8 * nrun) || hd.rp_off != hd.panel_off + 16 * nq * hd.h ||
+            hd.val_off != hd.rp_off || hd.meta_off != hd.val_off + 32 * ((ns + 7) / 8) ||
+            hd.bytes != hd.meta_off + 16 * ((ns + 7) / 8))
+            return fail(SABLE_ERR_INVALID, "layout: item %zu part offsets", k);
+        const unsigned char *R = L.records.data() + r.off;
+        int64_t total = 0;
+        for (int64_t i = 0; i < nrun; ++i) {
+            int32_t run[2];
+            memcpy(run, R + hd.runs_off + 8 * i, 8);
+            if (run[1] < 1 || run[0] < -1 || (run[0] >= 0 && (int64_t)run[0] + run[1] > L.n_cols))
+                return fail(SABLE_ERR_INVALID, "layout: item %zu window run", k);
+            total += run[1];
+        }
+        if (total != nw) return fail(SABLE_ERR_INVALID, "layout: item %zu window length", k);
+        const uint16_t *meta = reinterpret_cast<const uint16_t *>(R + hd.meta_off);
+        for (int64_t i = 0; i < ns; ++i) {
+            const int pos = meta[i] & 1023, row = meta[i] >> 10;
+            if (pos < 4 * nq || pos >= nw) return fail(SABLE_ERR_INVALID, "layout: item %zu window position", k);
+            if (row >= hd.h || (i > 0 && row < (meta[i - 1] >> 10)))
+                return fail(SABLE_ERR_INVALID, "layout: item %zu CSR rows", k);
+        }
         if (hd.nitem < 1 || hd.kidx < 0 || hd.kidx >= hd.nitem) return fail(SABLE_ERR_INVALID, "layout: item %zu numbering", k);
         if (hd.nitem > 1 && (hd.tile < 0 || hd.tile >= L.n_split_tiles || hd.part_base < 0 ||
                              hd.part_base + (int64_t)hd.nitem * hd.h > L.n_partial))
@@ -416,7 +650,7 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
         delete p;
         return fail(SABLE_ERR_ARG, "split_layout %d unknown", o.split_layout);
     }
-    rc = build_layout(desc, row_tile, chunk_bytes, o.split_layout, L);
+    rc = build_layout(desc, row_tile, chunk_bytes, o.split_layout, L, o.schedule == SABLE_SCHEDULE_WARP_ITEMS);
     if (rc) { delete p; return rc; }
     rc = plan_upload(p, L);
     if (rc) { sable_plan_destroy(p); return rc; }
@@ -438,7 +672,8 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
     const int split_layout = opts ? opts->split_layout : 0;
     if (split_layout != 0 && split_layout != 1) return fail(SABLE_ERR_ARG, "split_layout %d unknown", split_layout);
     Layout L;
-    rc = build_layout(desc, row_tile, chunk_bytes, split_layout, L);
+    rc = build_layout(desc, row_tile, chunk_bytes, split_layout, L,
+                      opts && opts->schedule == SABLE_SCHEDULE_WARP_ITEMS);
     if (rc) return rc;
     memset(out, 0, sizeof *out);
     out->n_tiles = L.n_tiles;

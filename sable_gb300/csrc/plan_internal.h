@@ -19,15 +19,19 @@ struct Layout {
     int32_t n_split_tiles = 0;
     std::vector<SplitTile> splits;        // split tiles (counter index order)
     int max_item_bytes = 0;
-    int max_xg_floats = 0;      // largest 4 nq + ns over items
+    int max_xg_floats = 0;      // largest 4 nq + ns over items (compact records: largest window)
+    bool compact = false;       // records are CompactHeader records (per-warp SpMV executor)
 };
 
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 int set_device(int dev);
 int validate_vbrc(const sable_vbrc_desc *d);
-int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int split_layout, Layout &L);
+// compact: CompactHeader records for the per-warp SpMV executor (schedule 2).
+int build_layout(const sable_vbrc_desc *d, int row_tile, int item_bytes, int split_layout, Layout &L,
+                 bool compact = false);
 int check_layout(const Layout &L);
+int check_compact_layout(const Layout &L);
 // Persistent schedule: tiles' items grouped into parts of <= part_bytes,
 // parts assigned to n_workers warp workers by greedy LPT (schedule.cpp).
 int build_warp_schedule(const Layout &L, int n_workers, int64_t part_bytes, std::vector<WorkRef> &work,
@@ -45,6 +49,7 @@ struct sable_plan {
     WorkRef *d_work = nullptr;           // warp-worker lists (persistent schedule)
     int *d_cta_begin = nullptr;          // worker ranges into d_work
     int n_ctas = 0;                      // warp workers of the persistent schedule
+    bool compact = false;                // compact records: SpMV through the per-warp executor only
     float *d_ppartial = nullptr;         // multi-part tile partials
     int *d_pcounters = nullptr;          // multi-part tile counters
     int64_t n_parts = 0, n_multi = 0;

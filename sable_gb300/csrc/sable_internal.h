@@ -20,11 +20,28 @@
 //             quad holds 4 columns of one row, so consecutive threads read
 //             consecutive 16-byte words while every thread keeps its row.
 //             One TMA bulk copy brings a whole item into shared memory.
+//             Plans of the per-warp SpMV executor (schedule 2) hold compact
+//             records instead (CompactHeader below), on tiles of at most
+//             SABLE_CW_MAX_ROWS rows: x is addressed through a per-item
+//             window of at most SABLE_CW_MAX positions given as column runs,
+//             and every CSR entry stores its window position and its row:
+//
+//               CompactHeader                    64 bytes
+//               runs   int2[nrun]  (16 B padded) (first x column, length); column -1: zeros
+//               panel  float4[nq*h]              as above; window positions [0, 4nq)
+//               val    float[ns]  (8-entry padded)  CSR values, row-major
+//               meta   uint16[ns] (8-entry padded)  window position | tile row << 10
+//
+//             Window positions [0, 4nq) are the panel columns, [4nq, nw) the
+//             columns of the item's CSR entries (sorted, runs closer than
+//             SABLE_CW_GAP columns merged).  A warp gathers the window into
+//             shared memory once per item with coalesced loads.
 //   table     int64 offset / bytes of each item, and per persistent CTA the
 //             [begin, end) range of its items (greedy LPT over item bytes).
 //   Split tiles publish per-item partial row sums; the last-arriving CTA
 //   adds them in item order (deterministic, no atomics on y).
 #pragma once
+#include <stddef.h>
 #include <stdint.h>
 
 #define SABLE_MAX_ROW_TILE 128
@@ -57,6 +74,35 @@ struct __align__(16) ItemHeader {
     int32_t mat;        // matrix index inside a batch (0 for a single plan)
 };
 static_assert(sizeof(ItemHeader) == 64, "ItemHeader must stay 64 bytes");
+
+#define SABLE_CW_MAX 1024     // window positions of a compact record (x floats a warp stages; 10 bits)
+#define SABLE_CW_MAX_ROWS 64  // rows of a compact tile (6 bits of a CSR entry's meta word)
+#define SABLE_CW_GAP 8        // CSR column runs closer than this share one window run
+
+// Header of a compact record.  Every field an ItemHeader also has sits at the
+// same offset, so the host code that reads tile / split fields reads both.
+struct __align__(16) CompactHeader {
+    int32_t row0, h, nq, ns;
+    int32_t runs_off;   // byte offsets of the record's parts
+    int32_t panel_off;
+    int32_t rp_off;     // = val_off (no row pointers: each entry carries its row)
+    int32_t val_off;
+    int32_t tile, kidx, nitem;
+    int32_t meta_off;
+    int64_t part_base;
+    int32_t bytes;
+    int16_t nrun;       // window runs
+    int16_t nw;         // window positions (<= SABLE_CW_MAX)
+};
+static_assert(sizeof(CompactHeader) == 64, "CompactHeader must stay 64 bytes");
+static_assert(offsetof(CompactHeader, h) == offsetof(ItemHeader, h) &&
+                  offsetof(CompactHeader, panel_off) == offsetof(ItemHeader, panel_off) &&
+                  offsetof(CompactHeader, rp_off) == offsetof(ItemHeader, rp_off) &&
+                  offsetof(CompactHeader, tile) == offsetof(ItemHeader, tile) &&
+                  offsetof(CompactHeader, nitem) == offsetof(ItemHeader, nitem) &&
+                  offsetof(CompactHeader, part_base) == offsetof(ItemHeader, part_base) &&
+                  offsetof(CompactHeader, bytes) == offsetof(ItemHeader, bytes),
+              "CompactHeader shares ItemHeader's field offsets");
 
 struct ItemRef {        // item table entry
     int64_t off;        // byte offset of the record

@@ -69,6 +69,7 @@ extern "C" int sable_spmm_noalloc(sable_plan *p, const float *X_dev, int64_t ldx
                     (long long)ldx, (long long)ldy);
     if (((uintptr_t)X_dev & 15) || ((uintptr_t)Y_dev & 15))
         return fail(SABLE_ERR_UNSUPPORTED, "SpMM operands must be 16-byte aligned");
+    if (p->compact) return fail(SABLE_ERR_UNSUPPORTED, "a plan of the per-warp SpMV executor (schedule 2) runs SpMV only");
     int rc = set_device(p->device);
     if (rc) return rc;
     int nt = 4;

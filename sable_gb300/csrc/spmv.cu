@@ -80,132 +80,188 @@ spmv_items_kernel(const LaunchArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// One warp per work item (schedule 2).  The record is read straight from HBM
-// with coalesced 16-byte streaming loads: no shared-memory staging, no TMA
-// wait and no CTA barrier, so every warp of the SM is an independent stream
-// and the SM keeps as many loads in flight as it has warps.  Dense panel:
-// for h <= 32 a warp step covers floor(32/h) quads (lane = (row, quad
-// offset)), for h > 32 lanes own rows lane, lane+32, ...; four quads per
-// step, their loads issued before any is used; the x values of the panel
-// columns are gathered once per item into shared memory.  CSR entries: in
-// chunks (warp_csr_chunks) into a per-warp row buffer in shared memory
-// (warp-synchronous only).  The
-// items of a split tile store partial row sums and the last one to arrive
-// adds them, so a launch needs no combine pass.
+// One warp per work item (schedule 2), over compact records.  The record is
+// read straight from HBM with coalesced streaming loads after one bulk L2
+// prefetch: no shared-memory staging of the record, no TMA wait and no CTA
+// barrier, so every warp of the SM is an independent stream.  The item's x
+// window (panel columns, then the columns of its CSR entries) is gathered
+// once into shared memory from its column runs, so neither part waits on a
+// column index before its x load.  Dense panel: for h <= 32 a warp step
+// covers floor(32/h) quads (lane = (row, quad offset)), for h > 32 lanes own
+// rows lane, lane+32, ...; four quads per step, their loads issued before
+// any is used.  CSR entries: in chunks of 256 (values and 16-bit window
+// positions) into a per-warp row buffer in shared memory (warp-synchronous
+// only).  The items of a split tile store partial row sums and the last one
+// to arrive adds them, so a launch needs no combine pass.
 // ---------------------------------------------------------------------------
-constexpr int WI_WARPS = 8;
-constexpr int WI_XG = 1024;  // x values of an item's panel columns gathered per warp (floats)
-constexpr int WI_CSR = 256;  // CSR entries per chunk of the per-warp CSR pass (8 per lane)
+constexpr int WI_WARPS = 4;       // warps (one item each) per CTA of the per-warp executor
+constexpr int WI_XW = SABLE_CW_MAX;  // x window floats per warp
+constexpr int WI_GU = 8;          // window positions per lane in flight while gathering
 
-// CSR entries of a warp's item in chunks of WI_CSR: every lane loads its 8
-// entries of the chunk and then their 8 x values (all independent: two
-// memory round trips per chunk), stores the products in `prod`, and the rows
-// are then summed from shared memory by groups of g lanes (g = 32 / h rounded
-// down to a power of two, at least 1), chunk after chunk, in a fixed order.
-// Adds each row's sum into rows[r].
-__device__ __forceinline__ void warp_csr_chunks(const int *rp, const uint2 *E, int h, int ns, int lane,
-                                                const float *__restrict__ x, float *rows, float *prod) {
-    int g = 32;
-    while (g > 1 && g * h > 32) g >>= 1;
-    const int gpw = 32 / g, sg = lane / g, sl = lane % g;
-    for (int c0 = 0; c0 < ns; c0 += WI_CSR) {
-        const int c1 = min(ns, c0 + WI_CSR);
-        uint2 en[WI_CSR / 32];
+__device__ __forceinline__ float4 ld_stream(const float4 *p) { return __ldcs(p); }
+
+// One bulk L2 prefetch of a whole record (16-byte aligned, a multiple of 16
+// bytes): DRAM sees one large request per item, and the warp's own loads of
+// the record hit L2 instead of each waiting a DRAM round trip.
+__device__ __forceinline__ void prefetch_record(const unsigned char *R, int bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(R), "r"((unsigned)bytes) : "memory");
+}
+
+// The x window of a compact record into xw[0, nw).  Runs are taken 32 at a
+// time, one per lane; every lane finds the run of each of its positions by a
+// binary search over the lanes' run starts (shuffles only), and keeps WI_GU
+// x loads in flight.  A run with column -1 reads as zeros.
+__device__ __forceinline__ void gather_window(const int2 *runs, int nrun, const float *__restrict__ x, float *xw,
+                                              int lane) {
+    int wbase = 0;
+    for (int r0 = 0; r0 < nrun; r0 += 32) {
+        const int nr = min(32, nrun - r0);
+        const int2 run = lane < nr ? runs[r0 + lane] : make_int2(0, 0);
+        int incl = run.y;
 #pragma unroll
-        for (int u = 0; u < WI_CSR / 32; ++u) {
-            const int e = c0 + lane + 32 * u;
-            en[u] = e < c1 ? E[e] : make_uint2(0u, 0u);
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += t;
         }
-        float xv[WI_CSR / 32];
+        const int start = wbase + incl - run.y;
+        const int key = lane < nr ? start : 0x7fffffff;  // lanes without a run never match
+        const int bend = __shfl_sync(FULL, wbase + incl, 31);
+        for (int p0 = wbase; p0 < bend; p0 += 32 * WI_GU) {
+            float v[WI_GU];
 #pragma unroll
-        for (int u = 0; u < WI_CSR / 32; ++u) {
-            const int e = c0 + lane + 32 * u;
-            xv[u] = e < c1 ? __ldg(x + en[u].y) : 0.f;
-        }
+            for (int u = 0; u < WI_GU; ++u) {
+                const int p = p0 + lane + 32 * u;
+                int j = 0;
 #pragma unroll
-        for (int u = 0; u < WI_CSR / 32; ++u) prod[lane + 32 * u] = __uint_as_float(en[u].x) * xv[u];
-        __syncwarp();
-        for (int r0 = 0; r0 < h; r0 += gpw) {
-            const int r = r0 + sg;
-            int b = 0, e = 0;
-            if (r < h) {
-                b = max(rp[r], c0) - c0;
-                e = min(rp[r + 1], c1) - c0;
+                for (int step = 16; step >= 1; step >>= 1)
+                    if (__shfl_sync(FULL, key, j + step) <= p) j += step;
+                const int c0 = __shfl_sync(FULL, run.x, j), s0 = __shfl_sync(FULL, start, j);
+                v[u] = (p < bend && c0 >= 0) ? __ldg(x + c0 + (p - s0)) : 0.f;
             }
-            float sum = 0.f;
-            for (int i = b + sl; i < e; i += g) sum += prod[i];
-            for (int o = g >> 1; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
-            if (sl == 0 && r < h && e > b) rows[r] += sum;
+#pragma unroll
+            for (int u = 0; u < WI_GU; ++u) {
+                const int p = p0 + lane + 32 * u;
+                if (p < bend) xw[p] = v[u];
+            }
+        }
+        wbase = bend;
+    }
+}
+
+// CSR entries of a compact record, 256 per warp step: lane l takes the 8
+// consecutive entries 8l..8l+7 of the step (two 16-byte value loads, one
+// 16-byte load of their meta words), multiplies each value by its x from
+// the window and sums the products by row in registers.  Entries are sorted
+// by row, so a lane's entries form a few row segments: a segment that starts
+// and ends inside the lane is complete and is added to rows[] at once; the
+// lane's last segment enters a segmented scan over the lanes (a segment
+// starts at a lane whose last segment began inside it, or whose row differs
+// from the previous lane's), and the lane that ends a scan segment adds its
+// total plus the next lane's first segment when that continues the row.
+// Every row of a step is added to rows[] by exactly one lane, and all sums
+// run in a fixed order.  Entries past ns take row CW_NOROW and are dropped.
+constexpr int CW_NOROW = 127;
+
+__device__ __forceinline__ void warp_csr_window(const float *val, const uint16_t *meta, int ns, int lane,
+                                                const float *xw, float *rows) {
+    for (int c0 = 0; c0 < ns; c0 += 256) {
+        const int e0 = c0 + 8 * lane;  // the record holds whole groups of 8 up to ns
+        float v[8];
+        int r[8];
+        if (e0 < ns) {
+            const float4 va = *reinterpret_cast<const float4 *>(val + e0);
+            const float4 vb = *reinterpret_cast<const float4 *>(val + e0 + 4);
+            const uint4 mw = *reinterpret_cast<const uint4 *>(meta + e0);
+            const unsigned m[4] = {mw.x, mw.y, mw.z, mw.w};
+            const float vv[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const unsigned mk = (m[k >> 1] >> (16 * (k & 1))) & 0xffffu;
+                const bool live = e0 + k < ns;
+                v[k] = live ? vv[k] * xw[mk & 1023u] : 0.f;
+                r[k] = live ? (int)(mk >> 10) : CW_NOROW;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                v[k] = 0.f;
+                r[k] = CW_NOROW;
+            }
+        }
+        // row segments inside the lane
+        int rf = r[0], rl = r[0];
+        float sf = 0.f, sl = v[0];
+        bool multi = false;
+#pragma unroll
+        for (int k = 1; k < 8; ++k) {
+            if (r[k] == rl) {
+                sl += v[k];
+            } else {
+                if (!multi) sf = sl;                    // the first segment ends
+                else if (rl < CW_NOROW) rows[rl] += sl;  // a middle segment: complete, this lane's alone
+                multi = true;
+                rl = r[k];
+                sl = v[k];
+            }
+        }
+        if (!multi) sf = sl;
+        // segmented inclusive scan of the lanes' last segments
+        const int prev_rl = __shfl_up_sync(FULL, rl, 1);
+        const bool head = lane == 0 || multi || prev_rl != rl;
+        float acc = sl;
+        bool flag = head;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float t = __shfl_up_sync(FULL, acc, o);
+            const bool f = __shfl_up_sync(FULL, flag, o);
+            if (lane >= o && !flag) {
+                acc += t;
+                flag = f;
+            }
+        }
+        const bool next_head = __shfl_down_sync(FULL, head, 1);
+        const bool next_multi = __shfl_down_sync(FULL, multi, 1);
+        const int next_rf = __shfl_down_sync(FULL, rf, 1);
+        const float next_sf = __shfl_down_sync(FULL, sf, 1);
+        // the first segment of a multi-segment lane: added here when it starts
+        // a row, by the previous lane when it continues the previous lane's row
+        if (multi && rf < CW_NOROW && (lane == 0 || prev_rl != rf)) rows[rf] += sf;
+        if ((lane == 31 || next_head) && rl < CW_NOROW) {
+            const bool cont = lane < 31 && next_multi && next_rf == rl;
+            rows[rl] += cont ? acc + next_sf : acc;
         }
         __syncwarp();
     }
 }
 
-__device__ __forceinline__ float4 ld_stream(const float4 *p) { return __ldcs(p); }
-
+// One compact work item by one warp (every lane calls it with the same
+// item): the x window into shared memory, CSR entries into the tile's rows,
+// the panel quads against the window, and the rows written to y or, for a
+// split tile, to the item's partial rows, the last of the tile's items adding
+// them into y.  rows: SABLE_CW_MAX_ROWS floats, xw: WI_XW floats of the
+// warp's shared memory.  TIMED: SM cycles of the item into a.cycles[item].
 template <bool TIMED>
-__global__ void __launch_bounds__(WI_WARPS * 32, 4)
-spmv_warp_items_kernel(const LaunchArgs a) {
-    __shared__ float s_rows[WI_WARPS][SABLE_MAX_ROW_TILE];  // CSR row sums of each warp's item
-    __shared__ __align__(16) float s_xg[WI_WARPS][WI_XG];     // x of each warp's panel columns
-    __shared__ float s_prod[WI_WARPS][WI_CSR];                // CSR products of one chunk
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int item = blockIdx.x * WI_WARPS + w;
-    if (item >= a.n_items) return;  // the whole warp leaves; no CTA barrier follows
+__device__ __forceinline__ void warp_item(const LaunchArgs &a, int item, int64_t off, int bytes, int lane, float *rows,
+                                          float *xw) {
     long long t0 = 0;
     if (TIMED && lane == 0) t0 = clock64();
-    const ItemRef ref = a.items[item];
-    const unsigned char *R = a.records + ref.off;
-    // One bulk L2 prefetch of the whole record (16-byte aligned, multiple of
-    // 16 bytes): DRAM sees one large request per item, and the warp's own
-    // loads below hit L2 instead of each waiting a DRAM round trip.
-    if (lane == 0)
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(R), "r"((unsigned)ref.bytes) : "memory");
-    const ItemHeader hd = *reinterpret_cast<const ItemHeader *>(R);
-    if (hd.bytes != ref.bytes || hd.h < 1 || hd.h > SABLE_MAX_ROW_TILE) {
+    const unsigned char *R = a.records + off;
+    const CompactHeader hd = *reinterpret_cast<const CompactHeader *>(R);
+    if (hd.bytes != bytes || hd.h < 1 || hd.h > SABLE_CW_MAX_ROWS || hd.nw > WI_XW) {
         if (lane == 0) atomicExch(a.error, 1);
         return;
     }
-    const MatIO &io = mat_of(a, hd.mat);
-    const float *__restrict__ x = io.x;
+    const MatIO &io = a.mat0;
     const int h = hd.h, nq = hd.nq, ns = hd.ns;
-    const int4 *xc = reinterpret_cast<const int4 *>(R + hd.xcol_off);
-    const float4 *P = reinterpret_cast<const float4 *>(R + hd.panel_off);
-    float *rows = s_rows[w];
+    __syncwarp();  // the previous item's reads of rows / xw are done
     for (int i = lane; i < h; i += 32) rows[i] = 0.f;
-    // x of the panel columns, gathered once for the item: all lanes issue
-    // their column-index and x loads together (GU per lane in flight), so the
-    // quad loop below waits on panel loads only.
-    const bool xg_ok = 4 * nq <= WI_XG;
-    float *xg = s_xg[w];
-    if (xg_ok) {
-        constexpr int GU = 8;
-        const int *xcol = reinterpret_cast<const int *>(xc);
-        for (int base = lane; base < 4 * nq; base += 32 * GU) {
-            float v[GU];
-#pragma unroll
-            for (int u = 0; u < GU; ++u) {
-                const int k = base + 32 * u;
-                v[u] = k < 4 * nq ? __ldg(x + __ldg(xcol + k)) : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < GU; ++u) {
-                const int k = base + 32 * u;
-                if (k < 4 * nq) xg[k] = v[u];
-            }
-        }
-    }
+    gather_window(reinterpret_cast<const int2 *>(R + hd.runs_off), hd.nrun, io.x, xw, lane);
     __syncwarp();
-    const float4 *xg4 = reinterpret_cast<const float4 *>(xg);
-    auto xq = [&](int q) { return xg_ok ? xg4[q] : xquad(xc, q, x); };
-    if (ns > 0) {
-        const int *rp = reinterpret_cast<const int *>(R + hd.rp_off);
-        const uint2 *E = reinterpret_cast<const uint2 *>(R + hd.csr_off);
-        // short tiles: chunked entries (many lanes per row); tall tiles: a
-        // lane group per row, where a chunk would leave one lane per row
-        if (h <= 16) warp_csr_chunks(rp, E, h, ns, lane, x, rows, s_prod[w]);
-        else csr_rows(rp, E, h, hd.g, 0, ns, lane, rows, [&](int, unsigned col) { return __ldg(x + col); });
-    }
+    if (ns > 0)
+        warp_csr_window(reinterpret_cast<const float *>(R + hd.val_off), reinterpret_cast<const uint16_t *>(R + hd.meta_off),
+                        ns, lane, xw, rows);
+    const float4 *P = reinterpret_cast<const float4 *>(R + hd.panel_off);
+    const float4 *xw4 = reinterpret_cast<const float4 *>(xw);
     auto put = [&](int i, float v) {
         if (hd.nitem <= 1) io.y[hd.row0 + i] = v;
         else io.partial[hd.part_base + (int64_t)hd.kidx * h + i] = v;
@@ -218,50 +274,40 @@ spmv_warp_items_kernel(const LaunchArgs a) {
             for (; q + 3 * qpw < nq; q += 4 * qpw) {
                 const float4 p0 = ld_stream(P + q * h + r), p1 = ld_stream(P + (q + qpw) * h + r);
                 const float4 p2 = ld_stream(P + (q + 2 * qpw) * h + r), p3 = ld_stream(P + (q + 3 * qpw) * h + r);
-                const float4 x0 = xq(q), x1 = xq(q + qpw);
-                const float4 x2 = xq(q + 2 * qpw), x3 = xq(q + 3 * qpw);
-                a0 = dot4(p0, x0, a0);
-                a1 = dot4(p1, x1, a1);
-                a0 = dot4(p2, x2, a0);
-                a1 = dot4(p3, x3, a1);
+                a0 = dot4(p0, xw4[q], a0);
+                a1 = dot4(p1, xw4[q + qpw], a1);
+                a0 = dot4(p2, xw4[q + 2 * qpw], a0);
+                a1 = dot4(p3, xw4[q + 3 * qpw], a1);
             }
-            for (; q < nq; q += qpw) a0 = dot4(ld_stream(P + q * h + r), xq(q), a0);
+            for (; q < nq; q += qpw) a0 = dot4(ld_stream(P + q * h + r), xw4[q], a0);
         }
         const float v = a0 + a1;
         float tot = 0.f;
         for (int k = 0; k < qpw; ++k) tot += __shfl_sync(FULL, v, r + k * h);  // fixed order over the quad offsets
         __syncwarp();
         if (lane < h) put(lane, tot + rows[lane]);
-    } else {
-        const bool v1 = lane + 32 < h, v2 = lane + 64 < h, v3 = lane + 96 < h;
-        float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f;
+    } else {  // 32 < h <= 64: lanes own rows lane and lane + 32
+        const bool v1 = lane + 32 < h;
+        float c0 = 0.f, c1 = 0.f;
         int q = 0;
         for (; q + 1 < nq; q += 2) {
-            const float4 xa = xq(q), xb = xq(q + 1);
+            const float4 xa = xw4[q], xb = xw4[q + 1];
             const float4 *Pa = P + q * h + lane, *Pb = Pa + h;
             const float4 pa0 = ld_stream(Pa), pb0 = ld_stream(Pb);
-            float4 pa1 = make_float4(0.f, 0.f, 0.f, 0.f), pb1 = pa1, pa2 = pa1, pb2 = pa1, pa3 = pa1, pb3 = pa1;
+            float4 pa1 = make_float4(0.f, 0.f, 0.f, 0.f), pb1 = pa1;
             if (v1) { pa1 = ld_stream(Pa + 32); pb1 = ld_stream(Pb + 32); }
-            if (v2) { pa2 = ld_stream(Pa + 64); pb2 = ld_stream(Pb + 64); }
-            if (v3) { pa3 = ld_stream(Pa + 96); pb3 = ld_stream(Pb + 96); }
             c0 = dot4(pb0, xb, dot4(pa0, xa, c0));
             c1 = dot4(pb1, xb, dot4(pa1, xa, c1));
-            c2 = dot4(pb2, xb, dot4(pa2, xa, c2));
-            c3 = dot4(pb3, xb, dot4(pa3, xa, c3));
         }
         if (q < nq) {
-            const float4 xa = xq(q);
+            const float4 xa = xw4[q];
             const float4 *Pa = P + q * h + lane;
             c0 = dot4(ld_stream(Pa), xa, c0);
             if (v1) c1 = dot4(ld_stream(Pa + 32), xa, c1);
-            if (v2) c2 = dot4(ld_stream(Pa + 64), xa, c2);
-            if (v3) c3 = dot4(ld_stream(Pa + 96), xa, c3);
         }
         __syncwarp();
         put(lane, c0 + rows[lane]);
         if (v1) put(lane + 32, c1 + rows[lane + 32]);
-        if (v2) put(lane + 64, c2 + rows[lane + 64]);
-        if (v3) put(lane + 96, c3 + rows[lane + 96]);
     }
     if (hd.nitem > 1) {
         // Split tile: the last of its items to arrive adds all partials in
@@ -290,6 +336,20 @@ spmv_warp_items_kernel(const LaunchArgs a) {
         __syncwarp();
         if (lane == 0) a.cycles[item] = (int64_t)(clock64() - t0);
     }
+}
+
+// One compact item per warp, in item-table order (largest first).
+template <bool TIMED>
+__global__ void __launch_bounds__(WI_WARPS * 32, 32 / WI_WARPS)
+spmv_warp_items_kernel(const LaunchArgs a) {
+    __shared__ float s_rows[WI_WARPS][SABLE_CW_MAX_ROWS];  // CSR row sums of each warp's item
+    __shared__ __align__(16) float s_xw[WI_WARPS][WI_XW];    // x window of each warp's item
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int item = blockIdx.x * WI_WARPS + w;
+    if (item >= a.n_items) return;  // the whole warp leaves; no CTA barrier follows
+    const ItemRef ref = a.items[item];
+    if (lane == 0) prefetch_record(a.records + ref.off, ref.bytes);
+    warp_item<TIMED>(a, item, ref.off, ref.bytes, lane, s_rows[w], s_xw[w]);
 }
 
 __global__ void __launch_bounds__(256)

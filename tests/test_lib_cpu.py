@@ -82,10 +82,10 @@ def test_block_features_match_numpy():
     np.testing.assert_allclose(out, ref, rtol=1e-6)
 
 
-def dry_run(comp, row_tile=0, chunk_bytes=0, split_layout=0):
+def dry_run(comp, row_tile=0, chunk_bytes=0, split_layout=0, schedule=0):
     desc, keep = _lib.make_desc(comp)
     st = _lib.PlanStats()
-    opts = _lib.PlanOpts(row_tile, chunk_bytes, 0, -1, 0, split_layout)
+    opts = _lib.PlanOpts(row_tile, chunk_bytes, 0, -1, schedule, split_layout)
     _lib.check(_lib.load().sable_plan_dry_run(ctypes.byref(desc), ctypes.byref(opts), ctypes.byref(st)), "dry_run")
     return {k: getattr(st, k) for k, _ in st._fields_}
 
@@ -93,10 +93,12 @@ def dry_run(comp, row_tile=0, chunk_bytes=0, split_layout=0):
 @pytest.mark.parametrize("row_tile", [128, 64, 17, 1])
 @pytest.mark.parametrize("chunk_bytes", [0, 4096, 6000, 32768])
 @pytest.mark.parametrize("split_layout", [0, 1])
-def test_layout_builder_edge_shapes(row_tile, chunk_bytes, split_layout):
+@pytest.mark.parametrize("schedule", [0, 2])
+def test_layout_builder_edge_shapes(row_tile, chunk_bytes, split_layout, schedule):
     """Tall rows, width/height-1 partitions, empty rows, tiny work items:
-    the builder's own bounds check (check_layout) passes and every stored
-    value lands in the panel or the CSR segments exactly once."""
+    the builder's own bounds check (check_layout; for the per-warp executor's
+    compact records check_compact_layout) passes and every stored value lands
+    in the panel or the CSR segments exactly once."""
     rng = np.random.default_rng(1)
     rs, cs = np.array([1, 300, 5, 1, 64, 129, 7, 2, 40]), np.array([1, 3, 200, 1, 9, 33, 128, 2, 4, 77])
     present = rng.random((len(rs), len(cs))) < 0.6
@@ -105,7 +107,7 @@ def test_layout_builder_edge_shapes(row_tile, chunk_bytes, split_layout):
                        (r.random((h, w)) < 0.4))
     dense = rng.random(m.n_blocks) < 0.5
     comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense)
-    st = dry_run(comp, row_tile, chunk_bytes, split_layout)
+    st = dry_run(comp, row_tile, chunk_bytes, split_layout, schedule)
     bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
     assert st["dense_values"] == int(bt.size[dense].sum())
     assert st["sparse_nnz"] == (0 if comp.indptr is None else int(comp.indptr[-1]))
@@ -123,3 +125,9 @@ def test_layout_builder_100k():
     assert st["dense_values"] == int(bt.size[dense].sum())
     assert st["dense_padded"] < 1.02 * st["dense_values"]
     assert 15000 < m.n_blocks < 25000
+    # compact records (per-warp executor, 8-row tiles): x columns as runs and
+    # 6-byte CSR entries make the records smaller than the standard ones
+    std8 = dry_run(comp, 8, 32768)
+    cmp8 = dry_run(comp, 8, 32768, schedule=2)
+    assert cmp8["dense_values"] == st["dense_values"] and cmp8["sparse_nnz"] == st["sparse_nnz"]
+    assert cmp8["device_bytes"] < 0.95 * std8["device_bytes"]

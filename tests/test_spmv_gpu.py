@@ -119,6 +119,59 @@ def test_one_huge_block_row(cuda, schedule):
     assert oracle.report(y, y_ref, yabs)["pass"]
 
 
+ROW_LENGTHS = [0, 1, 2, 3, 7, 8, 9, 15, 16, 17, 31, 32, 33, 63, 64, 65, 255, 256, 257, 300, 0, 0, 5, 1]
+
+
+@pytest.mark.parametrize("row_tile", [8, 17, 32, 64, 128])
+@pytest.mark.parametrize("chunk_bytes", [4096, 32768])
+@pytest.mark.parametrize("dense_frac", [0.0, 0.5])
+def test_compact_csr_row_lengths(cuda, row_tile, chunk_bytes, dense_frac):
+    """The per-warp executor's CSR pass (8 entries per lane, 256 per warp
+    step, rows summed by a segmented scan over the lanes) on rows whose
+    lengths straddle the lane and step boundaries, with empty rows and rows
+    longer than a step; tiles of up to 64 rows (128 is capped)."""
+    rng = np.random.default_rng(41)
+    rs, cs = [64, 40, 3, 64], [600, 700, 350]
+
+    def fill(r, h, w, a, b):
+        v = r.uniform(-1, 1, (h, w)).astype(np.float32)
+        if r.random() < dense_frac:
+            return v
+        keep = np.zeros((h, w), bool)
+        for i in range(h):
+            n = min(ROW_LENGTHS[(i + 7 * a + 3 * b) % len(ROW_LENGTHS)], w)
+            keep[i, r.choice(w, n, replace=False)] = True
+        return v * keep
+
+    m = synth.assemble(rng, np.array(rs), np.array(cs), np.ones((len(rs), len(cs)), bool), fill)
+    x = synth.vector(m.n_cols, 42)
+    dense = np.zeros(m.n_blocks, bool) if dense_frac == 0 else rng.random(m.n_blocks) < dense_frac
+    plan, comp, y_ref, yabs = plan_and_ref(m, dense, x, row_tile=row_tile, chunk_bytes=chunk_bytes,
+                                           schedule="warp_items")
+    y = run(plan, x)
+    r = oracle.report(y, y_ref, yabs)
+    assert r["pass"], r
+    y2 = run(plan, x)  # split-tile counters reset themselves; same bits again
+    np.testing.assert_array_equal(y, y2)
+    plan.check()
+
+
+def test_compact_plan_is_spmv_only(cuda):
+    """A plan of the per-warp executor holds compact records: SpMM and
+    batching refuse it with SABLE_ERR_UNSUPPORTED instead of misreading them."""
+    import torch
+    from sable_gb300 import _lib
+    from sable_gb300.batch import Batch
+    m = synth.spmv_1000()
+    plan, comp, y_ref, yabs = plan_and_ref(m, np.ones(m.n_blocks, bool), synth.vector(m.n_cols, 1),
+                                           schedule="warp_items")
+    X = torch.zeros(m.n_cols, 8, device="cuda")
+    with pytest.raises(_lib.SableError, match="SpMV only"):
+        plan.spmm(X)
+    with pytest.raises(_lib.SableError, match="not batched"):
+        Batch([plan], [1])
+
+
 def test_deterministic_and_host_entry(cuda):
     import torch
     m = synth.spmv_1000()
