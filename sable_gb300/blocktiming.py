@@ -120,9 +120,9 @@ def _form_cycles(m: synth.VbrMatrix, dense: bool, N: int, reps: int, spmm_tc, ch
 
 
 # SpMV blocks are timed in the shape the autotuner picks for large matrices:
-# one warp per 32 KB work item, 8-row tiles.
+# one warp per 32 KB work item (compact records), 32-row tiles.
 SPMV_SCHEDULE = "warp_items"
-SPMV_ROW_TILE = 8
+SPMV_ROW_TILE = 32
 SPMV_CHUNK = 32768
 
 

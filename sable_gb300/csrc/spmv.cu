@@ -87,12 +87,14 @@ spmv_items_kernel(const LaunchArgs a) {
 // window (panel columns, then the columns of its CSR entries) is gathered
 // once into shared memory from its column runs, so neither part waits on a
 // column index before its x load.  Dense panel: for h <= 32 a warp step
-// covers floor(32/h) quads (lane = (row, quad offset)), for h > 32 lanes own
-// rows lane, lane+32, ...; four quads per step, their loads issued before
-// any is used.  CSR entries: in chunks of 256 (values and 16-bit window
-// positions) into a per-warp row buffer in shared memory (warp-synchronous
-// only).  The items of a split tile store partial row sums and the last one
-// to arrive adds them, so a launch needs no combine pass.
+// covers floor(32/h) quads (lane = (row, quad offset)), eight per lane in
+// flight; for 32 < h <= 64 lanes own rows lane and lane+32, two quads per
+// step.  CSR entries: 256 per warp step (8 per lane: values and 16-bit
+// window position / row words), the next step's loads issued before this
+// step's row sums, which a segmented scan over the lanes adds into a
+// per-warp row buffer in shared memory (warp-synchronous only).  The items
+// of a split tile store partial row sums and the last one to arrive adds
+// them, so a launch needs no combine pass.
 // ---------------------------------------------------------------------------
 constexpr int WI_WARPS = 4;       // warps (one item each) per CTA of the per-warp executor
 constexpr int WI_XW = SABLE_CW_MAX;  // x window floats per warp
@@ -109,10 +111,12 @@ __device__ __forceinline__ void prefetch_record(const unsigned char *R, int byte
 
 // The x window of a compact record into xw[0, nw).  Runs are taken 32 at a
 // time, one per lane; every lane finds the run of each of its positions by a
-// binary search over the lanes' run starts (shuffles only), and keeps WI_GU
-// x loads in flight.  A run with column -1 reads as zeros.
+// binary search over the lanes' run starts (shuffles only; the WI_GU searches
+// of a lane are independent, so they overlap), and keeps WI_GU x loads in
+// flight.  A run with column -1 reads as zeros.
 __device__ __forceinline__ void gather_window(const int2 *runs, int nrun, const float *__restrict__ x, float *xw,
                                               int lane) {
+    constexpr int ZERO = -(1 << 30);  // column offset of a zero run: offset + position < 0
     int wbase = 0;
     for (int r0 = 0; r0 < nrun; r0 += 32) {
         const int nr = min(32, nrun - r0);
@@ -124,19 +128,20 @@ __device__ __forceinline__ void gather_window(const int2 *runs, int nrun, const 
             if (lane >= o) incl += t;
         }
         const int start = wbase + incl - run.y;
-        const int key = lane < nr ? start : 0x7fffffff;  // lanes without a run never match
+        const int key = lane < nr ? start : 0x7fffffff;                     // lanes without a run never match
+        const int coff = (lane < nr && run.x >= 0) ? run.x - start : ZERO;  // x column = coff + position
         const int bend = __shfl_sync(FULL, wbase + incl, 31);
         for (int p0 = wbase; p0 < bend; p0 += 32 * WI_GU) {
             float v[WI_GU];
 #pragma unroll
             for (int u = 0; u < WI_GU; ++u) {
                 const int p = p0 + lane + 32 * u;
-                int j = 0;
+                int j = 0;  // last lane whose run starts at or before p
 #pragma unroll
                 for (int step = 16; step >= 1; step >>= 1)
                     if (__shfl_sync(FULL, key, j + step) <= p) j += step;
-                const int c0 = __shfl_sync(FULL, run.x, j), s0 = __shfl_sync(FULL, start, j);
-                v[u] = (p < bend && c0 >= 0) ? __ldg(x + c0 + (p - s0)) : 0.f;
+                const int col = __shfl_sync(FULL, coff, j) + p;
+                v[u] = (p < bend && col >= 0) ? __ldg(x + col) : 0.f;
             }
 #pragma unroll
             for (int u = 0; u < WI_GU; ++u) {
@@ -154,24 +159,39 @@ __device__ __forceinline__ void gather_window(const int2 *runs, int nrun, const 
 // the window and sums the products by row in registers.  Entries are sorted
 // by row, so a lane's entries form a few row segments: a segment that starts
 // and ends inside the lane is complete and is added to rows[] at once; the
-// lane's last segment enters a segmented scan over the lanes (a segment
-// starts at a lane whose last segment began inside it, or whose row differs
-// from the previous lane's), and the lane that ends a scan segment adds its
-// total plus the next lane's first segment when that continues the row.
+// lanes' last segments are summed by a scan inside each group of lanes that
+// end on the same row, and the group's last lane adds the total plus the
+// next lane's first segment when that continues the row.
 // Every row of a step is added to rows[] by exactly one lane, and all sums
 // run in a fixed order.  Entries past ns take row CW_NOROW and are dropped.
 constexpr int CW_NOROW = 127;
 
 __device__ __forceinline__ void warp_csr_window(const float *val, const uint16_t *meta, int ns, int lane,
                                                 const float *xw, float *rows) {
+    // raw loads of a step (the record holds whole groups of 8 up to ns)
+    auto fetch = [&](int c0, float4 &va, float4 &vb, uint4 &mw) {
+        const int e0 = c0 + 8 * lane;
+        if (e0 < ns) {
+            va = *reinterpret_cast<const float4 *>(val + e0);
+            vb = *reinterpret_cast<const float4 *>(val + e0 + 4);
+            mw = *reinterpret_cast<const uint4 *>(meta + e0);
+        } else {
+            va = vb = make_float4(0.f, 0.f, 0.f, 0.f);
+            mw = make_uint4(0u, 0u, 0u, 0u);
+        }
+    };
+    float4 va, vb;
+    uint4 mw;
+    fetch(0, va, vb, mw);
     for (int c0 = 0; c0 < ns; c0 += 256) {
-        const int e0 = c0 + 8 * lane;  // the record holds whole groups of 8 up to ns
+        // the next step's loads go out before this step's sums (one step ahead)
+        float4 na = va, nb = vb;
+        uint4 nm = mw;
+        if (c0 + 256 < ns) fetch(c0 + 256, na, nb, nm);
+        const int e0 = c0 + 8 * lane;
         float v[8];
         int r[8];
-        if (e0 < ns) {
-            const float4 va = *reinterpret_cast<const float4 *>(val + e0);
-            const float4 vb = *reinterpret_cast<const float4 *>(val + e0 + 4);
-            const uint4 mw = *reinterpret_cast<const uint4 *>(meta + e0);
+        {
             const unsigned m[4] = {mw.x, mw.y, mw.z, mw.w};
             const float vv[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
 #pragma unroll
@@ -181,13 +201,10 @@ __device__ __forceinline__ void warp_csr_window(const float *val, const uint16_t
                 v[k] = live ? vv[k] * xw[mk & 1023u] : 0.f;
                 r[k] = live ? (int)(mk >> 10) : CW_NOROW;
             }
-        } else {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                v[k] = 0.f;
-                r[k] = CW_NOROW;
-            }
         }
+        va = na;
+        vb = nb;
+        mw = nm;
         // row segments inside the lane
         int rf = r[0], rl = r[0];
         float sf = 0.f, sl = v[0];
@@ -205,31 +222,24 @@ __device__ __forceinline__ void warp_csr_window(const float *val, const uint16_t
             }
         }
         if (!multi) sf = sl;
-        // segmented inclusive scan of the lanes' last segments
-        const int prev_rl = __shfl_up_sync(FULL, rl, 1);
-        const bool head = lane == 0 || multi || prev_rl != rl;
+        // The lanes whose last segment is row rl form one contiguous group
+        // (rows never decrease along the entries): an inclusive scan inside
+        // the group leaves the group's total in its last lane.
+        const unsigned grp = __match_any_sync(FULL, rl);
+        const int gfirst = __ffs(grp) - 1, glast = 31 - __clz(grp);
         float acc = sl;
-        bool flag = head;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const float t = __shfl_up_sync(FULL, acc, o);
-            const bool f = __shfl_up_sync(FULL, flag, o);
-            if (lane >= o && !flag) {
-                acc += t;
-                flag = f;
-            }
+            if (lane - o >= gfirst) acc += t;
         }
-        const bool next_head = __shfl_down_sync(FULL, head, 1);
-        const bool next_multi = __shfl_down_sync(FULL, multi, 1);
-        const int next_rf = __shfl_down_sync(FULL, rf, 1);
-        const float next_sf = __shfl_down_sync(FULL, sf, 1);
-        // the first segment of a multi-segment lane: added here when it starts
-        // a row, by the previous lane when it continues the previous lane's row
-        if (multi && rf < CW_NOROW && (lane == 0 || prev_rl != rf)) rows[rf] += sf;
-        if ((lane == 31 || next_head) && rl < CW_NOROW) {
-            const bool cont = lane < 31 && next_multi && next_rf == rl;
-            rows[rl] += cont ? acc + next_sf : acc;
-        }
+        // The first segment of a multi-segment lane: added here when it
+        // starts a row, by the previous lane's group when it continues it.
+        const int prev_rl = __shfl_up_sync(FULL, rl, 1);
+        const bool cont = multi && lane > 0 && prev_rl == rf;
+        const float to_prev = __shfl_down_sync(FULL, cont ? sf : 0.f, 1);
+        if (multi && !cont && rf < CW_NOROW) rows[rf] += sf;
+        if (lane == glast && rl < CW_NOROW) rows[rl] += lane < 31 ? acc + to_prev : acc;
         __syncwarp();
     }
 }
@@ -271,6 +281,16 @@ __device__ __forceinline__ void warp_item(const LaunchArgs &a, int item, int64_t
         float a0 = 0.f, a1 = 0.f;
         if (lane < qpw * h) {
             int q = sidx;
+            for (; q + 7 * qpw < nq; q += 8 * qpw) {  // 8 quads per lane in flight
+                float4 p[8];
+#pragma unroll
+                for (int k = 0; k < 8; ++k) p[k] = ld_stream(P + (q + k * qpw) * h + r);
+#pragma unroll
+                for (int k = 0; k < 8; k += 2) {
+                    a0 = dot4(p[k], xw4[q + k * qpw], a0);
+                    a1 = dot4(p[k + 1], xw4[q + (k + 1) * qpw], a1);
+                }
+            }
             for (; q + 3 * qpw < nq; q += 4 * qpw) {
                 const float4 p0 = ld_stream(P + q * h + r), p1 = ld_stream(P + (q + qpw) * h + r);
                 const float4 p2 = ld_stream(P + (q + 2 * qpw) * h + r), p3 = ld_stream(P + (q + 3 * qpw) * h + r);
