@@ -146,9 +146,7 @@ def choices(m, bt, N: int):
     from sable_gb300 import blockmodel, convert
     feats = convert.block_features(m.val, bt, N)
     rf = blockmodel.RFTableModel().choose_dense(feats)
-    mlp = blockmodel.MLPModel.load()
-    p = mlp.predict(feats)
-    return feats, rf, p[:, 0] < p[:, 1]
+    return feats, rf, blockmodel.MLPModel.load().choose_dense(feats)
 
 
 def build_workload(rank: int):

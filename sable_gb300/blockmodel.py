@@ -17,9 +17,14 @@ variance, N):
                    models/convert_rf_pkl.py with a whitelisting unpickler.
   MLPModel         the learned cost model: MLP 6 -> 64 -> 64 -> 2 predicting
                    the log2 device time (SM cycles) of the dense and of the
-                   sparse form of a block; dense iff t_dense < t_sparse.  Its
-                   inference is libsable's batched kernel (sable_mlp_infer),
-                   on the GPU only.
+                   sparse form of a block.  A form's cost is its predicted
+                   cycles plus, for SpMV (N = 1), kappa_spmv cycles per byte
+                   it stores: in a bandwidth-bound launch every byte a block
+                   adds also delays the other items sharing DRAM, which its
+                   own item cycles do not show.  kappa_spmv is measured with
+                   the timings (cycles per byte of large dense blocks).  Dense
+                   iff cost_dense < cost_sparse.  Its inference is libsable's
+                   batched kernel (sable_mlp_infer), on the GPU only.
 default_model() returns the MLP when its weights file exists and a GPU is
 present, else the RandomForest table (the reference threshold), as the
 fallback.
@@ -173,9 +178,17 @@ class MLPModel:
                                                    torch.cuda.current_stream().cuda_stream), "sable_mlp_infer")
         return out.cpu().numpy()
 
+    @property
+    def kappa_spmv(self) -> float:
+        return float(self.meta.get("kappa_spmv", 0.0))
+
+    def costs(self, feats: np.ndarray) -> np.ndarray:
+        """[n, 2] cost (cycles) of the dense and of the sparse form."""
+        return decision_costs(self.predict(feats), feats, self.kappa_spmv)
+
     def choose_dense(self, feats: np.ndarray) -> np.ndarray:
-        p = self.predict(feats)
-        return p[:, 0] < p[:, 1]
+        c = self.costs(feats)
+        return c[:, 0] < c[:, 1]
 
     def __del__(self):
         try:
@@ -205,6 +218,25 @@ def init_params(seed: int = 0) -> np.ndarray:
     p = np.concatenate(parts).astype(np.float32)
     assert p.size == _lib.MLP_NPARAMS
     return p
+
+
+def stored_bytes(feats: np.ndarray) -> np.ndarray:
+    """[n, 2] bytes the dense and the sparse form of a block store: 4 h w
+    dense; CSR 6 nnz in the per-warp SpMV executor's compact records (N = 1),
+    8 nnz + 4 (h + 1) in the standard records of SpMM."""
+    f = np.asarray(feats, dtype=np.float64)
+    sparse = np.where(f[:, 5] == 1, 6 * f[:, 2], 8 * f[:, 2] + 4 * (f[:, 0] + 1))
+    return np.stack([4 * f[:, 0] * f[:, 1], sparse], 1)
+
+
+def decision_costs(log2_cycles: np.ndarray, feats: np.ndarray, kappa_spmv: float) -> np.ndarray:
+    """[n, 2] decision cost of both forms from predicted (or measured)
+    log2(1 + cycles): cycles, plus kappa_spmv cycles per stored byte for SpMV
+    blocks (feature N = 1)."""
+    cyc = np.exp2(np.asarray(log2_cycles, dtype=np.float64)) - 1.0
+    f = np.asarray(feats, dtype=np.float64)
+    bw = np.where((f[:, 5] == 1)[:, None], kappa_spmv * stored_bytes(f), 0.0)
+    return cyc + bw
 
 
 def byte_rule(feats: np.ndarray) -> np.ndarray:

@@ -11,10 +11,16 @@
 2. Targets: log2(1 + cycles) of both forms.  80 % of the blocks train the
    network with libsable's own kernels (Adam, sable_mlp_train_step); 20 %
    are held out.
-3. Reports on the held-out blocks the regret of each choice rule against the
-   measured-best form — the MLP, the reference RandomForest (the fallback),
-   the byte rule, fixed density thresholds — overall and per N, and writes
-   the weights, normalisation and these figures to --out.
+3. kappa_spmv: the median cycles per stored byte of the large (>= 50 KB)
+   dense SpMV blocks of the training part, the cost of a byte when DRAM is
+   saturated.  SpMV decisions add it per stored byte to the predicted cycles
+   (blockmodel.decision_costs).
+4. Reports on the held-out blocks the regret of each choice rule against the
+   measured-best form — the MLP (pure cycle prediction, and its decision rule
+   with the byte term, measured by cycles + kappa_spmv x bytes), the
+   reference RandomForest (the fallback), the byte rule, fixed density
+   thresholds — overall and per N, and writes the weights, normalisation,
+   kappa_spmv and these figures to --out.
 Needs a CUDA device; prints one JSON summary line last.
 """
 from __future__ import annotations
@@ -66,11 +72,19 @@ def main(argv=None) -> int:
                        log=log)
     t_train = time.time() - t1
     model = blockmodel.MLPModel(trainer.params(), mean, std)
+    ftr = feats[tr]
+    big = (ftr[:, 5] == 1) & (4 * ftr[:, 0] * ftr[:, 1] >= 50000)
+    kappa = float(np.median(cd[tr][big] / (4 * ftr[big, 0] * ftr[big, 1]))) if big.any() else 0.0
 
     ft, dt, st = feats[te], cd[te], cs[te]
     pred = model.predict(ft)
+    # SpMV blocks measured by cycles + kappa x stored bytes: the decision cost
+    sv = ft[:, 5] == 1
+    meas = blockmodel.decision_costs(np.log2(1.0 + np.stack([dt, st], 1)), ft, kappa)
+    dec = blockmodel.decision_costs(pred, ft, kappa)
     rules = {
         "mlp": pred[:, 0] < pred[:, 1],
+        "mlp_decision": dec[:, 0] < dec[:, 1],
         "rf_reference": blockmodel.RFTableModel().choose_dense(ft),
         "byte_rule": blockmodel.byte_rule(ft),
         "all_dense": np.ones(len(te), bool),
@@ -86,9 +100,14 @@ def main(argv=None) -> int:
     for N in (1, 8, 32, 128):
         sel = ft[:, 5] == N
         summary["regret_by_N"][str(N)] = {k: blockmodel.regret(v[sel], dt[sel], st[sel]) for k, v in rules.items()}
+    summary["kappa_spmv"] = kappa
+    summary["regret_spmv_decision_cost"] = {k: blockmodel.regret(v[sv], meas[sv, 0], meas[sv, 1])
+                                            for k, v in rules.items()}
     model.meta = {"trained_on": "synthetic blocks_200k timings (SM cycles, GB300)", "blocks": n,
                   "regret_mlp": summary["regret"]["mlp"], "regret_rf": summary["regret"]["rf_reference"],
-                  "regret_byte_rule": summary["regret"]["byte_rule"], "epochs": a.epochs}
+                  "regret_byte_rule": summary["regret"]["byte_rule"], "epochs": a.epochs, "kappa_spmv": kappa,
+                  "regret_mlp_spmv_decision": summary["regret_spmv_decision_cost"]["mlp_decision"],
+                  "regret_rf_spmv_decision": summary["regret_spmv_decision_cost"]["rf_reference"]}
     model.save(a.out)
     print(json.dumps(summary))
     return 0

@@ -51,8 +51,22 @@ def test_regret_and_rules():
     np.testing.assert_array_equal(blockmodel.byte_rule(f), [True, False])
 
 
+def test_decision_costs():
+    """Stored bytes per form (compact 6-byte CSR entries for SpMV, standard
+    8-byte entries + row pointers for SpMM) and the byte term of the SpMV
+    decision cost."""
+    f = np.array([[10, 20, 50, 0.25, 0, 1], [10, 20, 50, 0.25, 0, 32]], np.float32)
+    np.testing.assert_array_equal(blockmodel.stored_bytes(f), [[800, 300], [800, 444]])
+    lc = np.log2(1.0 + np.array([[100.0, 200.0], [100.0, 200.0]]))
+    c = blockmodel.decision_costs(lc, f, 2.0)
+    np.testing.assert_allclose(c, [[100 + 1600, 200 + 600], [100, 200]])  # no byte term for SpMM
+
+
 def test_committed_model_file():
     z = np.load(blockmodel.MLP_FILE)
     assert z["params"].shape == (mlp_oracle.NPARAMS,) and np.all(np.isfinite(z["params"]))
     assert np.all(z["std"] > 0)
     assert float(z["regret_mlp"]) <= 0.05 < float(z["regret_rf"])
+    # the SpMV decision rule's byte term: measured, plausible, and its regret
+    assert 0.5 < float(z["kappa_spmv"]) < 8.0
+    assert float(z["regret_mlp_spmv_decision"]) <= 0.05 < float(z["regret_rf_spmv_decision"])

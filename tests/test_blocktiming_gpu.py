@@ -32,3 +32,12 @@ def test_trained_model_gains_over_reference_threshold(cuda):
     r_rf = blockmodel.regret(rf.choose_dense(feats), cd, cs)
     assert r_mlp <= 0.05, (r_mlp, r_rf)
     assert r_rf > 3 * r_mlp, (r_mlp, r_rf)
+    # the plans' decision rule (cycles + kappa_spmv x stored bytes for SpMV):
+    # within 5 % by cycles, and by its own cost on the SpMV blocks
+    dec = model.choose_dense(feats)
+    assert blockmodel.regret(dec, cd, cs) <= 0.05
+    sv = feats[:, 5] == 1
+    meas = blockmodel.decision_costs(np.log2(1.0 + np.stack([cd, cs], 1)), feats, model.kappa_spmv)
+    r_dec = blockmodel.regret(dec[sv], meas[sv, 0], meas[sv, 1])
+    r_rf_dec = blockmodel.regret(rf.choose_dense(feats)[sv], meas[sv, 0], meas[sv, 1])
+    assert r_dec <= 0.05 and r_rf_dec > 3 * r_dec, (r_dec, r_rf_dec)
