@@ -295,7 +295,11 @@ def run_sable(args):
     plain = Plan(comp_p)
     xd = torch.as_tensor(x).cuda()
     yd = torch.empty(m.n_rows, dtype=torch.float32, device="cuda")
-    learned = autotune.tune(comp_l, xd, yd, N=1)
+    if args.shape:  # a fixed per-warp shape instead of the autotuner (kernel profiles)
+        rt, cb = (int(v) for v in args.shape.split(","))
+        learned = autotune._build(comp_l, {"executor": "warp_items", "row_tile": rt, "chunk_bytes": cb}, 1, "split3")
+    else:
+        learned = autotune.tune(comp_l, xd, yd, N=1)
     flush = autotune.l2_flush
 
     with ClockSampler(local) as clk:
@@ -427,6 +431,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline SpMV only (no SpMM / batch sections)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--shape", help="ROW_TILE,CHUNK_BYTES: run the headline on the per-warp executor in this shape "
+                                    "instead of autotuning (for kernel profiles)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
