@@ -73,7 +73,8 @@ typedef struct sable_vbrc_desc {
 
 /* Plan layout options; zero-initialise for defaults. */
 typedef struct sable_plan_opts {
-    int32_t row_tile;     /* rows per tile, 1..128 (0: 128)                    */
+    int32_t row_tile;     /* rows per tile, 1..128 (0: 128; schedule 2 caps
+                             tiles at 64 rows)                                 */
     int32_t chunk_bytes;  /* target matrix bytes per work item, 4096..78643
                              (0: 32768; 8192 for schedule 1, 16384 for 2)     */
     int32_t spmm_tc;      /* dense blocks of SpMM with N >= 32 on the tensor
@@ -86,8 +87,11 @@ typedef struct sable_plan_opts {
     int32_t schedule;     /* 0: one CTA per work item (TMA-staged record);
                              1: persistent warp workers over an LPT schedule
                              of tile parts, each with a private TMA ring;
-                             2: one warp per work item, record read with
-                             coalesced 16-byte loads, no CTA barrier           */
+                             2: one warp per work item over compact records
+                             (x columns as runs, CSR entries of 6 bytes),
+                             read with coalesced loads, no CTA barrier; an
+                             SpMV-only plan: SpMM, the no-allocation SpMM and
+                             batches return SABLE_ERR_UNSUPPORTED for it    */
     int32_t split_layout; /* a row tile larger than one work item is cut into
                              0: items that each take a share of the tile's
                                 dense quads and of its CSR entries (SpMV runs

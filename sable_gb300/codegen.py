@@ -37,9 +37,9 @@ from .plan import Plan
 
 # Launch shapes the entry points use unless plan options say otherwise: the
 # fastest shapes measured on large matrices (one warp per 32 KB work item over
-# 32-row tiles for SpMV; one CTA per work item with separate dense and CSR
+# 16-row tiles for SpMV; one CTA per work item with separate dense and CSR
 # items for SpMM).  sable_gb300.autotune picks per matrix.
-SPMV_SHAPE = {"schedule": "warp_items", "row_tile": 32, "chunk_bytes": 32768}
+SPMV_SHAPE = {"schedule": "warp_items", "row_tile": 16, "chunk_bytes": 32768}
 SPMM_SHAPE = {"split_layout": "separate"}
 
 
