@@ -294,17 +294,41 @@ int sable_spmv_timed(sable_plan *plan, const float *x_dev, float *y_dev, int64_t
     return run_spmv(plan, x_dev, y_dev, cycles_dev, stream);
 }
 
+// Device address of pinned (page-locked, mapped) host memory, or nullptr for
+// any other pointer (pageable memory, device memory).
+static void *mapped_host(const void *ptr) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int sable_spmv_host(sable_plan *p, const float *x_host, float *y_host, void *stream) {
     if (!p || !x_host || !y_host) return fail(SABLE_ERR_ARG, "null argument");
     int rc = set_device(p->device);
     if (rc) return rc;
     if ((rc = ensure_host_staging(p, p->n_cols, p->n_rows))) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e = cudaMemcpyAsync(p->d_x, x_host, (size_t)p->n_cols * sizeof(float), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return cuda_fail(e, "copy x to device");
-    if ((rc = run_spmv(p, p->d_x, p->d_y, nullptr, stream))) return rc;
-    e = cudaMemcpyAsync(y_host, p->d_y, (size_t)p->n_rows * sizeof(float), cudaMemcpyDeviceToHost, s);
-    if (e != cudaSuccess) return cuda_fail(e, "copy y to host");
+    // Pinned host buffers are read and written by the kernels themselves
+    // (one copy kernel for x, the SpMV's own stores for y): no copy-engine
+    // transfer and its setup on either side.  Other buffers go through
+    // cudaMemcpyAsync and the plan's device staging.
+    const float *xm = static_cast<const float *>(mapped_host(x_host));
+    float *ym = static_cast<float *>(mapped_host(y_host));
+    cudaError_t e = cudaSuccess;
+    if (xm) {
+        if ((rc = launch_copy_floats(p->d_x, xm, p->n_cols, stream))) return cuda_fail((cudaError_t)rc, "copy x to device");
+    } else {
+        e = cudaMemcpyAsync(p->d_x, x_host, (size_t)p->n_cols * sizeof(float), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return cuda_fail(e, "copy x to device");
+    }
+    if ((rc = run_spmv(p, p->d_x, ym ? ym : p->d_y, nullptr, stream))) return rc;
+    if (!ym) {
+        e = cudaMemcpyAsync(y_host, p->d_y, (size_t)p->n_rows * sizeof(float), cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return cuda_fail(e, "copy y to host");
+    }
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "stream synchronize");
     return SABLE_OK;

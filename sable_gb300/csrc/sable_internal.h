@@ -169,6 +169,8 @@ int launch_spmv_items(const LaunchArgs &a, bool timed, void *stream);
 int launch_spmv_warp_items(const LaunchArgs &a, bool timed, void *stream);
 // y rows of split tiles from their items' partial sums (after the items ran).
 int launch_spmv_combine(const SplitTile *tiles, int n_tiles, const MatIO *mats, const MatIO &mat0, void *stream);
+// dst[0, n) = src[0, n) by a kernel (either side may be mapped host memory).
+int launch_copy_floats(float *dst, const float *src, int64_t n, void *stream);
 int launch_spmv_warps(const LaunchArgs &a, int n_workers, void *stream);
 int spmv_items_smem(int stage_bytes, int xg_floats);
 int spmv_warp_smem(int stage_bytes, int xg_floats);

@@ -26,6 +26,7 @@
 // All sums run in a fixed order: results are bitwise reproducible.
 // Every mbarrier wait is bounded (2 s); on expiry the plan's error flag is
 // set and the worker waits (bounded again) for its own copies, then returns.
+#include <algorithm>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "sable_internal.h"
@@ -372,6 +373,22 @@ spmv_warp_items_kernel(const LaunchArgs a) {
     warp_item<TIMED>(a, item, ref.off, ref.bytes, lane, s_rows[w], s_xw[w]);
 }
 
+// dst[0, n) = src[0, n) (either side may be mapped host memory): 16-byte
+// loads and stores when both are 16-byte aligned, grid-stride.
+__global__ void __launch_bounds__(256)
+copy_floats_kernel(float *__restrict__ dst, const float *__restrict__ src, int64_t n) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if ((((uintptr_t)dst | (uintptr_t)src) & 15) == 0) {
+        const int64_t n4 = n / 4;
+        for (int64_t k = i; k < n4; k += stride)
+            reinterpret_cast<float4 *>(dst)[k] = reinterpret_cast<const float4 *>(src)[k];
+        done = 4 * n4;
+    }
+    for (int64_t k = done + i; k < n; k += stride) dst[k] = src[k];
+}
+
 __global__ void __launch_bounds__(256)
 spmv_combine_kernel(const SplitTile *__restrict__ tiles, int n, const MatIO *mats, const MatIO mat0) {
     const int t = blockIdx.x * 8 + (threadIdx.x >> 5);
@@ -634,6 +651,13 @@ int launch_spmv_warp_items(const LaunchArgs &a, bool timed, void *stream) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (timed) spmv_warp_items_kernel<true><<<grid, WI_WARPS * 32, 0, s>>>(a);
     else spmv_warp_items_kernel<false><<<grid, WI_WARPS * 32, 0, s>>>(a);
+    return (int)cudaGetLastError();
+}
+
+int launch_copy_floats(float *dst, const float *src, int64_t n, void *stream) {
+    if (n <= 0) return 0;
+    const int64_t blocks = std::min<int64_t>((n / 4 + 255) / 256 + 1, 1024);
+    copy_floats_kernel<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(dst, src, n);
     return (int)cudaGetLastError();
 }
 
