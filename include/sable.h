@@ -133,7 +133,10 @@ int sable_spmv(sable_plan *plan, const float *x_dev, float *y_dev, void *stream)
  * if a bounded device-side wait of an earlier launch of this plan ran out. */
 int sable_plan_check(sable_plan *plan, void *stream);
 
-/* Same, from host buffers: copies x in, runs, copies y out, synchronises. */
+/* Same, from host buffers: copies x in, runs, copies y out, synchronises.
+ * Pinned (page-locked) buffers are read and written by the kernels
+ * themselves; pageable ones are copied with cudaMemcpyAsync through the
+ * plan's device staging buffers. */
 int sable_spmv_host(sable_plan *plan, const float *x_host, float *y_host, void *stream);
 
 /* Executor, SpMM: Y = A X with X row-major n_cols x N (leading dimension
