@@ -35,6 +35,9 @@ SPMV_CANDIDATES = [
 ]
 SPMM_CANDIDATES = [
     {"executor": "items", "row_tile": rt, "chunk_bytes": cb} for rt in (128, 64) for cb in (16384, 32768, 49152, 65536)
+] + [
+    # items above the shared-memory staging size: SpMM-only plans, long K loops, no split tiles
+    {"executor": "items", "row_tile": 128, "chunk_bytes": cb} for cb in (131072, 262144)
 ] + [{"executor": "ring", "row_tile": 128, "chunk_bytes": 32768, "stages": 2}]
 
 _cache: dict[str, dict] = {}

@@ -324,6 +324,9 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
         if (plans[i]->device != plans[0]->device) return fail(SABLE_ERR_ARG, "plans on different devices");
         if (plans[i]->compact)
             return fail(SABLE_ERR_UNSUPPORTED, "plan %d: a plan of the per-warp SpMV executor (schedule 2) is not batched", i);
+        if (!plans[i]->staged_ok)
+            return fail(SABLE_ERR_UNSUPPORTED, "plan %d: work items larger than the batch's staging (%d bytes)", i,
+                        SABLE_MAX_ITEM_BYTES);
         if (widths[i] < 1 || (widths[i] > 1 && (widths[i] & 3)))
             return fail(SABLE_ERR_UNSUPPORTED, "width %d of matrix %d: 1, or a multiple of 4", widths[i], i);
     }

@@ -89,9 +89,11 @@ int plan_upload(sable_plan *p, const Layout &L) {
     // Plans whose items are too large for a warp worker's ring run one CTA per item.
     if (p->schedule == SABLE_SCHEDULE_PERSISTENT && spmv_warp_smem(p->max_item_bytes, p->max_xg_floats) > dev_max)
         p->schedule = SABLE_SCHEDULE_ITEMS;
-    if (spmv_items_smem(p->max_item_bytes, p->max_xg_floats + 4) > dev_max)
-        return fail(SABLE_ERR_UNSUPPORTED, "work items need %d bytes of shared memory (device: %d)",
-                    spmv_items_smem(p->max_item_bytes, p->max_xg_floats + 4), dev_max);
+    // Records too large to stage in shared memory (items above ~96 KB, for
+    // SpMM's long K loops) leave an SpMM-only plan: the SpMM kernels stream
+    // records in K steps, the SpMV and batch executors stage whole records.
+    p->staged_ok = p->compact || (p->max_item_bytes <= SABLE_MAX_ITEM_BYTES &&
+                                  spmv_items_smem(p->max_item_bytes, p->max_xg_floats + 4) <= dev_max);
     p->stats.n_tiles = L.n_tiles;
     p->stats.n_chunks = p->n_items;
     p->stats.dense_values = L.dense_values;
@@ -129,6 +131,9 @@ LaunchArgs spmv_args(const sable_plan *p, const float *x, float *y, int64_t *cyc
 
 static int run_spmv(sable_plan *p, const float *x, float *y, int64_t *cycles, void *stream) {
     if (!p || !x || !y) return fail(SABLE_ERR_ARG, "null argument");
+    if (!p->staged_ok)
+        return fail(SABLE_ERR_UNSUPPORTED, "work items of %d bytes: an SpMM-only plan (SpMV stages items of at most %d bytes)",
+                    p->max_item_bytes, SABLE_MAX_ITEM_BYTES);
     int rc = set_device(p->device);
     if (rc) return rc;
     LaunchArgs a = spmv_args(p, x, y, cycles);

@@ -508,7 +508,7 @@ int check_layout(const Layout &L) {
     for (size_t k = 0; k < L.items.size(); ++k) {
         const ItemRef &r = L.items[k];
         if (r.off < 0 || (r.off & 15) || r.bytes < (int)sizeof(ItemHeader) || (r.bytes & 15) || r.off + r.bytes > nrec ||
-            r.bytes > SABLE_MAX_ITEM_BYTES)
+            r.bytes > SABLE_MAX_RECORD_BYTES)
             return fail(SABLE_ERR_INVALID, "layout: item %zu record range", k);
         ItemHeader hd;
         memcpy(&hd, L.records.data() + r.off, sizeof hd);
@@ -623,8 +623,9 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
                                              : o.schedule == SABLE_SCHEDULE_WARP_ITEMS ? SABLE_WARP_ITEMS_ITEM_BYTES
                                                                                        : SABLE_WARP_ITEM_BYTES);
     if (row_tile < 1 || row_tile > SABLE_MAX_ROW_TILE) return fail(SABLE_ERR_ARG, "row_tile %d outside 1..128", row_tile);
-    if (chunk_bytes < 4096 || chunk_bytes > SABLE_MAX_ITEM_BYTES * 4 / 5)
-        return fail(SABLE_ERR_ARG, "chunk_bytes %d outside 4096..%d", chunk_bytes, SABLE_MAX_ITEM_BYTES * 4 / 5);
+    const int max_chunk = o.schedule == SABLE_SCHEDULE_ITEMS ? SABLE_MAX_CHUNK_BYTES : SABLE_MAX_ITEM_BYTES * 4 / 5;
+    if (chunk_bytes < 4096 || chunk_bytes > max_chunk)
+        return fail(SABLE_ERR_ARG, "chunk_bytes %d outside 4096..%d", chunk_bytes, max_chunk);
     int rc = validate_vbrc(desc);
     if (rc) return rc;
     rc = set_device(o.device);
@@ -666,7 +667,9 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
                                : opts->schedule == SABLE_SCHEDULE_WARP_ITEMS ? SABLE_WARP_ITEMS_ITEM_BYTES
                                                                              : SABLE_WARP_ITEM_BYTES);
     if (row_tile < 1 || row_tile > SABLE_MAX_ROW_TILE) return fail(SABLE_ERR_ARG, "row_tile %d outside 1..128", row_tile);
-    if (chunk_bytes < 4096 || chunk_bytes > SABLE_MAX_ITEM_BYTES * 4 / 5) return fail(SABLE_ERR_ARG, "chunk_bytes outside range");
+    const int max_chunk = (!opts || opts->schedule == SABLE_SCHEDULE_ITEMS) ? SABLE_MAX_CHUNK_BYTES
+                                                                           : SABLE_MAX_ITEM_BYTES * 4 / 5;
+    if (chunk_bytes < 4096 || chunk_bytes > max_chunk) return fail(SABLE_ERR_ARG, "chunk_bytes outside range");
     int rc = validate_vbrc(desc);
     if (rc) return rc;
     const int split_layout = opts ? opts->split_layout : 0;

@@ -50,6 +50,7 @@ struct sable_plan {
     int *d_cta_begin = nullptr;          // worker ranges into d_work
     int n_ctas = 0;                      // warp workers of the persistent schedule
     bool compact = false;                // compact records: SpMV through the per-warp executor only
+    bool staged_ok = true;               // records fit the shared-memory staging of SpMV and batches
     float *d_ppartial = nullptr;         // multi-part tile partials
     int *d_pcounters = nullptr;          // multi-part tile counters
     int64_t n_parts = 0, n_multi = 0;

@@ -47,7 +47,9 @@
 #define SABLE_MAX_ROW_TILE 128
 #define SABLE_THREADS 256
 #define SABLE_NWARP (SABLE_THREADS / 32)
-#define SABLE_MAX_ITEM_BYTES 98304   // record bytes; bounds a TMA staging buffer
+#define SABLE_MAX_ITEM_BYTES 98304   // record bytes the SpMV / batch executors stage in shared memory
+#define SABLE_MAX_RECORD_BYTES (1 << 22)  // any record (SpMM streams records in K steps)
+#define SABLE_MAX_CHUNK_BYTES (1 << 20)   // chunk_bytes of one-CTA-per-item plans (larger items: SpMM only)
 #define SABLE_WSTAGES 2              // TMA ring depth of a persistent warp worker
 #define SABLE_ITEMS_ITEM_BYTES 32768 // default item size, one CTA per item
 #define SABLE_WARP_ITEM_BYTES 8192   // default item size, warp workers

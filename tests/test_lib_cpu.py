@@ -114,6 +114,18 @@ def test_layout_builder_edge_shapes(row_tile, chunk_bytes, split_layout, schedul
     assert st["dense_padded"] >= st["dense_values"]
 
 
+def test_large_items_schedule_0_only():
+    """chunk_bytes above the staging size: accepted for one CTA per item (an
+    SpMM-only plan), refused for the warp executors."""
+    m = synth.spmm_50k(n=4000, parts=80)
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, np.ones(m.n_blocks, bool))
+    st = dry_run(comp, 128, 262144)
+    assert st["n_chunks"] <= st["n_tiles"] + 2
+    for sched in (1, 2):
+        with pytest.raises(_lib.SableError):
+            dry_run(comp, 128, 262144, schedule=sched)
+
+
 def test_layout_builder_100k():
     """The 100000^2 workload builds, with < 2 % panel padding."""
     m = synth.spmv_100k()

@@ -85,3 +85,30 @@ def test_spmm_host_entry(cuda):
     Yd = plan.spmm(torch.as_tensor(X).cuda()).cpu().numpy()
     Yh = plan.spmm_host(X)
     np.testing.assert_array_equal(Yd, Yh)
+
+
+@pytest.mark.parametrize("N", [32, 128])
+@pytest.mark.parametrize("tc", [False, "split3"])
+def test_large_items_spmm_only(cuda, N, tc):
+    """Work items above the shared-memory staging size (256 KB: whole block
+    rows per item, long K loops, no split tiles): SpMM parity, and SpMV and
+    batching refuse the plan instead of staging records that do not fit."""
+    import torch
+    from sable_gb300 import _lib
+    from sable_gb300.batch import Batch
+    m = random_vbr(61, np.full(12, 120), np.full(20, 40), 0.5, dense_frac=0.7)  # ~0.1-0.2 MB per block row
+    X = synth.dense_operand(m.n_cols, N, 62)
+    rng = np.random.default_rng(63)
+    dense = rng.random(m.n_blocks) < 0.7
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense)
+    plan = Plan(comp, spmm_tc=tc, chunk_bytes=262144, split_layout="separate")
+    assert plan.stats()["scratch_floats"] == 0  # no tile is split
+    Y = plan.spmm(torch.as_tensor(X).cuda()).cpu().numpy()
+    Yr, Ya = oracle.spmm_vbr(m, X)
+    r = oracle.report(Y, Yr, Ya, tol_of(tc))
+    assert r["pass"], r
+    with pytest.raises(_lib.SableError, match="SpMM-only"):
+        plan.spmv(torch.zeros(m.n_cols, device="cuda"))
+    with pytest.raises(_lib.SableError, match="staging"):
+        Batch([plan], [N])
+    plan.close()
