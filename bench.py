@@ -282,6 +282,33 @@ def bench_batch(reps: int) -> dict:
                       "graph": True, "tuning": table}}
 
 
+def run_spmm_profile(args):
+    """The 50000^2 SpMM with the learned choice at one width and one launch
+    shape, a few launches, nothing else (a small case for kernel profiles)."""
+    import torch
+    from sable_gb300 import convert, synth
+    from sable_gb300.plan import Plan
+    N, rt, cb = (int(v) for v in args.spmm_profile.split(","))
+    m = synth.spmm_50k()
+    bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+    _, _, mlp = choices(m, bt, N)
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mlp, bt=bt)
+    plan = Plan(comp, row_tile=rt, chunk_bytes=cb, spmm_tc="split3", split_layout="separate")
+    X = torch.as_tensor(synth.dense_operand(m.n_cols, N, 7)).cuda()
+    Y = torch.empty(m.n_rows, N, device="cuda")
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        plan.spmm(X, Y)
+    s.record()
+    for _ in range(args.steps):
+        plan.spmm(X, Y)
+    e.record()
+    e.synchronize()
+    plan.check()
+    print(json.dumps({"spmm_profile": {"N": N, "row_tile": rt, "chunk_bytes": cb, "items": plan.stats()["n_chunks"],
+                                       "ms_per_launch": s.elapsed_time(e) / args.steps}}))
+
+
 def run_sable(args):
     import torch
     from sable_gb300 import _lib, autotune, blockmodel, convert
@@ -431,6 +458,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline SpMV only (no SpMM / batch sections)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--spmm-profile", help="N,ROW_TILE,CHUNK_BYTES: only run the 50000^2 SpMM (learned choice, "
+                                           "split BF16) in this shape, for kernel profiles")
     ap.add_argument("--shape", help="ROW_TILE,CHUNK_BYTES: run the headline on the per-warp executor in this shape "
                                     "instead of autotuning (for kernel profiles)")
     args = ap.parse_args()
@@ -438,6 +467,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.spmm_profile:
+        run_spmm_profile(args)
     else:
         run_sable(args)
 
