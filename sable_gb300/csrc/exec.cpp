@@ -2,6 +2,7 @@
 // launches (device and host-buffer forms), timed variants, error check.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "sable.h"
@@ -27,6 +28,8 @@ static int upload_vec(T **dptr, const T *h, size_t n, const char *what, int64_t 
     }
     return SABLE_OK;
 }
+
+static int build_tc_planes(sable_plan *p, const Layout &L, int64_t *bytes);
 
 
 int plan_upload(sable_plan *p, const Layout &L) {
@@ -99,9 +102,76 @@ int plan_upload(sable_plan *p, const Layout &L) {
     p->stats.dense_values = L.dense_values;
     p->stats.dense_padded = L.dense_padded;
     p->stats.sparse_nnz = L.sparse_nnz;
+    if (p->spmm_tc != SABLE_TC_OFF && !L.compact && (rc = build_tc_planes(p, L, &bytes))) return rc;
     p->stats.device_bytes = bytes;
     p->stats.scratch_floats = L.n_partial;
     return SABLE_OK;
+}
+
+// Round to nearest even FP32 -> BF16 (bit pattern); NaN stays a quiet NaN.
+static uint16_t bf16_rn(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+static float bf16_value(uint16_t b) {
+    const uint32_t u = (uint32_t)b << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+// Split-BF16 SpMM: every item's dense panel split once into BF16 terms
+// (t_k = bf16(v - t_0 - ... - t_{k-1}), round to nearest even, the same split
+// the tensor-core kernel otherwise does per K step) and laid out as the
+// m16n8k16 A fragments of each lane: for K step ks (16 panel columns) and M
+// tile mt (16 rows), TC_TERMS x 32 words of 16 bytes, word (ks, mt, term,
+// lane) = the four BF16 pairs (rows 16mt + g and + 8, columns 16ks + 2t,
+// + 1 and + 8, + 9; g = lane / 4, t = lane % 4; zero outside the panel).
+static int build_tc_planes(sable_plan *p, const Layout &L, int64_t *bytes) {
+    constexpr int TERMS = 3;
+    const std::vector<ItemRef> &table = p->items_host;
+    std::vector<int64_t> off(table.size(), 0);
+    std::vector<uint32_t> words;  // 4 per 16-byte word
+    for (size_t idx = 0; idx < table.size(); ++idx) {
+        const unsigned char *R = L.records.data() + table[idx].off;
+        ItemHeader hd;
+        memcpy(&hd, R, sizeof hd);
+        off[idx] = (int64_t)(words.size() / 4);
+        if (hd.nq <= 0) continue;
+        const float *P = reinterpret_cast<const float *>(R + hd.panel_off);
+        const int h = hd.h, ncol = 4 * hd.nq, nks = (ncol + 15) / 16, mtiles = (h + 15) / 16;
+        auto A = [&](int i, int c) -> float {
+            return (i < h && c < ncol) ? P[((int64_t)(c >> 2) * h + i) * 4 + (c & 3)] : 0.f;
+        };
+        const size_t base = words.size();
+        words.resize(base + (size_t)nks * mtiles * TERMS * 32 * 4, 0u);
+        for (int ks = 0; ks < nks; ++ks)
+            for (int mt = 0; mt < mtiles; ++mt)
+                for (int lane = 0; lane < 32; ++lane) {
+                    const int g = lane >> 2, t = lane & 3, r0 = 16 * mt + g, c0 = 16 * ks + 2 * t;
+                    const float v[4][2] = {{A(r0, c0), A(r0, c0 + 1)}, {A(r0 + 8, c0), A(r0 + 8, c0 + 1)},
+                                           {A(r0, c0 + 8), A(r0, c0 + 9)}, {A(r0 + 8, c0 + 8), A(r0 + 8, c0 + 9)}};
+                    for (int reg = 0; reg < 4; ++reg) {
+                        float a0 = v[reg][0], a1 = v[reg][1];
+                        for (int k = 0; k < TERMS; ++k) {
+                            const uint16_t b0 = bf16_rn(a0), b1 = bf16_rn(a1);
+                            a0 -= bf16_value(b0);
+                            a1 -= bf16_value(b1);
+                            const size_t w = base + ((((size_t)ks * mtiles + mt) * TERMS + k) * 32 + lane) * 4 + reg;
+                            words[w] = (uint32_t)b0 | ((uint32_t)b1 << 16);
+                        }
+                    }
+                }
+    }
+    if (words.empty()) return SABLE_OK;
+    int rc = upload_vec(reinterpret_cast<uint32_t **>(&p->d_tcplanes), words.data(), words.size(), "split-BF16 panels",
+                        bytes);
+    if (rc) return rc;
+    return upload_vec(&p->d_tcoff, off.data(), off.size(), "split-BF16 offsets", bytes);
 }
 
 LaunchArgs spmv_args(const sable_plan *p, const float *x, float *y, int64_t *cycles) {
@@ -210,6 +280,8 @@ static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_
     a.mat0.pad = std::max<int32_t>(p->n_split_tiles, 1);  // counters per N-slice
     a.cycles = cycles;
     a.error = p->d_error;
+    a.tcplanes = p->d_tcplanes;
+    a.tcoff = p->d_tcoff;
     a.n_items = (int)p->n_items;
     a.stage_bytes = p->max_item_bytes;
     const int64_t part_stride = p->n_partial * nt;

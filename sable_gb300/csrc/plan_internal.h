@@ -51,6 +51,8 @@ struct sable_plan {
     int n_ctas = 0;                      // warp workers of the persistent schedule
     bool compact = false;                // compact records: SpMV through the per-warp executor only
     bool staged_ok = true;               // records fit the shared-memory staging of SpMV and batches
+    void *d_tcplanes = nullptr;          // split-BF16 SpMM: pre-split A fragments (16-byte words)
+    int64_t *d_tcoff = nullptr;          // word offset of each item's fragments (item-table order)
     float *d_ppartial = nullptr;         // multi-part tile partials
     int *d_pcounters = nullptr;          // multi-part tile counters
     int64_t n_parts = 0, n_multi = 0;

@@ -160,6 +160,8 @@ struct LaunchArgs {
     const MatIO *mats;      // per matrix (batch); nullptr: every item uses mat0
     MatIO mat0;
     int64_t *cycles;        // per-item SM cycles (timed variant) or nullptr
+    const void *tcplanes;   // SpMM split-BF16: pre-split A fragments (uint4 words) or nullptr
+    const int64_t *tcoff;   // word offset of each item's fragments in tcplanes (item-table order)
     int *error;             // set to 1 when a bounded device wait runs out
     int n_items;
     int stage_bytes;        // TMA staging bytes per stage (>= largest record)

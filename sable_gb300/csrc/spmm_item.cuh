@@ -44,11 +44,13 @@
 //
 // Work item = (item record, N-slice of width NT <= 128), one CTA of 8 warps:
 //   K loop over the item's panel columns, 16 at a time: the 16 X rows of the
-//   panel columns (through the record's xcol table) and the 4 panel quads
-//   are staged in shared memory as FP32; every warp converts its A fragments
-//   (16 rows x 16 columns) and B fragments (16 x 8) to BF16 terms on the
-//   fly and issues 3 (TERMS = 2) or 6 (TERMS = 3) MMAs per 16 x 8 output tile.  Warps split the N-tiles
-//   first, then the M-tiles.
+//   panel columns (through the record's xcol table) are staged in shared
+//   memory as FP32, and so are the A fragments: pre-split (PRE, the plan's
+//   BF16 term fragments built once on the host, one 16-byte word per lane and
+//   term) or the 4 FP32 panel quads, which every warp then splits per K step
+//   (the batch kernel's form).  Every warp converts its B fragments (16 x 8)
+//   to BF16 terms and issues 3 (TERMS = 2) or 6 (TERMS = 3) MMAs per 16 x 8
+//   output tile.  Warps split the N-tiles first, then the M-tiles.
 //   The accumulators go to the Y tile in shared memory, the CSR entries are
 //   added by warp-owned row ranges (as in the FP32 kernel), and the tile is
 //   stored (split tiles: partial tiles + last-arriving CTA, in item order).
@@ -88,6 +90,34 @@ __device__ __forceinline__ void stage_kstep(float4 *Bs, float4 *As, int k0, int 
         const int qq = t / h, i = t - qq * h, q = qbase + qq;
         const bool ok = q < nq;
         cp16z(&As[qq * SABLE_MAX_ROW_TILE + i], ok ? P + (int64_t)q * h + i : P, ok);
+    }
+}
+
+// Pre-split A fragments (built with the plan): for every K step ks and M
+// tile mt of an item, TC_TERMS x 32 16-byte words in the order [ks][mt][term]
+// [lane]; word (ks, mt, term, lane) holds the four packed BF16 pairs of
+// lane's m16n8k16 A fragment of that term.
+constexpr int TC_TERMS = 3;
+
+// Starts the copies of the A fragments of K step ks (mtiles M tiles, all
+// terms) into one stage; a step past the item's last is zero-filled.
+__device__ __forceinline__ void stage_tc_planes(uint4 *Ap, const uint4 *planes, int ks, int nks, int mtiles) {
+    const int n = mtiles * TC_TERMS * 32;
+    const bool ok = ks < nks;
+    const uint4 *src = planes + (int64_t)(ok ? ks : 0) * n;
+    for (int t = threadIdx.x; t < n; t += SABLE_THREADS) cp16z(&Ap[t], ok ? src + t : planes, ok);
+}
+
+// Starts the copies of the KSTEP X rows of K step k0 only (pre-split A).
+template <int NT>
+__device__ __forceinline__ void stage_x_rows(float4 *Bs, int k0, int ncol, const int *colmap, const float *X,
+                                             int64_t ldx, int N, int n0) {
+    constexpr int CQ = NT / 4;
+    for (int t = threadIdx.x; t < KSTEP * CQ; t += SABLE_THREADS) {
+        const int kk = t / CQ, q = t - kk * CQ, k = k0 + kk, n = n0 + 4 * q;
+        const bool ok = k < ncol && n < N;
+        const float *src = ok ? X + (int64_t)__ldg(colmap + k) * ldx + n : X;
+        cp16z(&Bs[t], src, ok);
     }
 }
 
@@ -289,12 +319,13 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
-template <int NT>
+template <int NT, bool PRE = false>
 struct TcSmem {
     static constexpr int CQ = NT / 4;
     static constexpr int YS = SABLE_MAX_ROW_TILE * NT * 4;               // Y tile (FP32)
     static constexpr int BS = KSTEP * NT * 4;                            // staged X rows (FP32)
-    static constexpr int AS = (KSTEP / 4) * SABLE_MAX_ROW_TILE * 16;     // staged quads
+    static constexpr int AS = PRE ? (SABLE_MAX_ROW_TILE / 16) * TC_TERMS * 32 * 16  // staged A fragments
+                                  : (KSTEP / 4) * SABLE_MAX_ROW_TILE * 16;         // staged quads
     static constexpr int RST = (SABLE_MAX_ROW_TILE + 8) * 4;
     // The K-loop stages share the space of the Y tile, which is only used
     // after the loop.
@@ -305,10 +336,12 @@ struct TcSmem {
     static constexpr int TOTAL = OFF_RST + RST;
 };
 
-template <int NT, int TERMS>
+// PRE: the item's A fragments come pre-split (planes: the item's words, see
+// stage_tc_planes) instead of being split from the FP32 panel on every step.
+template <int NT, int TERMS, bool PRE = false>
 __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO &a, int slice, int64_t part_stride,
-                                             unsigned char *smem) {
-    using L = TcSmem<NT>;
+                                             unsigned char *smem, const uint4 *planes = nullptr) {
+    using L = TcSmem<NT, PRE>;
     constexpr int CQ = L::CQ;
     constexpr int NTILES = NT / 8;                        // 8-column MMA tiles of the slice
     constexpr int WN = NTILES < 4 ? NTILES : 4;           // warps along N (4 x 2 grid: each A fragment is
@@ -346,23 +379,31 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
 
     // KSTAGES-deep pipeline, as in spmm_fp32_item
     float4 *Bs4 = reinterpret_cast<float4 *>(Bs);
+    constexpr int ASTAGE = L::AS / 16;  // float4 / uint4 words of one A stage
+    uint4 *Ap = reinterpret_cast<uint4 *>(As);
+    const int nks = (ncol + KSTEP - 1) / KSTEP;
+    auto stage = [&](int k0, int sb) {
+        if (PRE) {
+            stage_x_rows<NT>(Bs4 + sb * (KSTEP * CQ), k0, ncol, colmap, X, a.ldx, a.N, n0);
+            stage_tc_planes(Ap + sb * ASTAGE, planes, k0 / KSTEP, nks, mtiles);
+        } else {
+            stage_kstep<NT>(Bs4 + sb * (KSTEP * CQ), As + sb * ASTAGE, k0, ncol, colmap, X, a.ldx, a.N, n0, P, h, nq);
+        }
+    };
     for (int st = 0; st < KSTAGES - 1; ++st) {
-        if (st * KSTEP < ncol)
-            stage_kstep<NT>(Bs4 + st * (KSTEP * CQ), As + st * ((KSTEP / 4) * SABLE_MAX_ROW_TILE), st * KSTEP, ncol,
-                            colmap, X, a.ldx, a.N, n0, P, h, nq);
+        if (st * KSTEP < ncol) stage(st * KSTEP, st);
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
     int buf = 0;
     for (int k0 = 0; k0 < ncol; k0 += KSTEP, buf = (buf + 1) % KSTAGES) {
         const int nk = k0 + (KSTAGES - 1) * KSTEP, nb = (buf + KSTAGES - 1) % KSTAGES;
-        if (nk < ncol)
-            stage_kstep<NT>(Bs4 + nb * (KSTEP * CQ), As + nb * ((KSTEP / 4) * SABLE_MAX_ROW_TILE), nk, ncol, colmap, X,
-                            a.ldx, a.N, n0, P, h, nq);
+        if (nk < ncol) stage(nk, nb);
         asm volatile("cp.async.commit_group;" ::: "memory");
         asm volatile("cp.async.wait_group %0;" :: "n"(KSTAGES - 1) : "memory");
         __syncthreads();
         const float *Bsb = Bs + buf * (KSTEP * NT);
-        const float *Af = reinterpret_cast<const float *>(As + buf * ((KSTEP / 4) * SABLE_MAX_ROW_TILE));
+        const float *Af = reinterpret_cast<const float *>(As + buf * ASTAGE);
+        const uint4 *Apb = Ap + buf * ASTAGE;
         // B fragments of this warp's N-tiles: bt[j][term][register]
         uint32_t bt[NPW][TERMS][2];
 #pragma unroll
@@ -390,25 +431,36 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
             const int mt = wm + i * WM;
             if (mt >= mtiles) continue;
             // A fragment rows r0 = 16 mt + g, r1 = r0 + 8; columns 2t, 2t+1 (+8)
-            const int r0 = mt * 16 + g, r1 = r0 + 8;
-            // column c of the K-step lives in quad c/4, component c%4: A(row, c) = Af[((c/4)*128 + row)*4 + c%4]
-            auto ld2 = [&](int row, int col) {
-                if (row >= h) return make_float2(0.f, 0.f);
-                return *reinterpret_cast<const float2 *>(Af + ((col >> 2) * SABLE_MAX_ROW_TILE + row) * 4 + (col & 3));
-            };
-            const float2 a00 = ld2(r0, 2 * t), a10 = ld2(r1, 2 * t), a01 = ld2(r0, 2 * t + 8), a11 = ld2(r1, 2 * t + 8);
-            uint32_t s00[TERMS], s10[TERMS], s01[TERMS], s11[TERMS];
-            split<TERMS>(a00.x, a00.y, s00);
-            split<TERMS>(a10.x, a10.y, s10);
-            split<TERMS>(a01.x, a01.y, s01);
-            split<TERMS>(a11.x, a11.y, s11);
             uint32_t at[TERMS][4];
+            if (PRE) {
 #pragma unroll
-            for (int k = 0; k < TERMS; ++k) {
-                at[k][0] = s00[k];
-                at[k][1] = s10[k];
-                at[k][2] = s01[k];
-                at[k][3] = s11[k];
+                for (int k = 0; k < TERMS; ++k) {
+                    const uint4 w = Apb[(mt * TC_TERMS + k) * 32 + lane];
+                    at[k][0] = w.x;
+                    at[k][1] = w.y;
+                    at[k][2] = w.z;
+                    at[k][3] = w.w;
+                }
+            } else {
+                const int r0 = mt * 16 + g, r1 = r0 + 8;
+                // column c of the K-step lives in quad c/4, component c%4: A(row, c) = Af[((c/4)*128 + row)*4 + c%4]
+                auto ld2 = [&](int row, int col) {
+                    if (row >= h) return make_float2(0.f, 0.f);
+                    return *reinterpret_cast<const float2 *>(Af + ((col >> 2) * SABLE_MAX_ROW_TILE + row) * 4 + (col & 3));
+                };
+                const float2 a00 = ld2(r0, 2 * t), a10 = ld2(r1, 2 * t), a01 = ld2(r0, 2 * t + 8), a11 = ld2(r1, 2 * t + 8);
+                uint32_t s00[TERMS], s10[TERMS], s01[TERMS], s11[TERMS];
+                split<TERMS>(a00.x, a00.y, s00);
+                split<TERMS>(a10.x, a10.y, s10);
+                split<TERMS>(a01.x, a01.y, s01);
+                split<TERMS>(a11.x, a11.y, s11);
+#pragma unroll
+                for (int k = 0; k < TERMS; ++k) {
+                    at[k][0] = s00[k];
+                    at[k][1] = s10[k];
+                    at[k][2] = s01[k];
+                    at[k][3] = s11[k];
+                }
             }
             // products in the order (a-term, b-term), smallest terms first; the
             // N-tile loop inside, so consecutive MMAs go to independent

@@ -10,7 +10,9 @@
 
 namespace {
 
-template <int NT, int TERMS, bool TIMED>
+// PRE: the plan's pre-split A fragments (la.tcplanes, la.tcoff) feed the
+// tensor cores; otherwise every warp splits its FP32 fragments per K step.
+template <int NT, int TERMS, bool TIMED, bool PRE>
 __global__ void __launch_bounds__(SABLE_THREADS)
 spmm_tc_kernel(const LaunchArgs la, const int64_t part_stride) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -19,20 +21,30 @@ spmm_tc_kernel(const LaunchArgs la, const int64_t part_stride) {
     const int item = blockIdx.x, slice = blockIdx.y;
     const unsigned char *R = la.records + la.items[item].off;
     const MatIO &a = mat_of(la, reinterpret_cast<const ItemHeader *>(R)->mat);
-    spmm_tc_item<NT, TERMS>(R, a, slice, part_stride, smem);
+    if (PRE)
+        spmm_tc_item<NT, TERMS, true>(R, a, slice, part_stride, smem,
+                                      static_cast<const uint4 *>(la.tcplanes) + la.tcoff[item]);
+    else
+        spmm_tc_item<NT, TERMS, false>(R, a, slice, part_stride, smem);
     if (TIMED) {
         __syncthreads();
         if (threadIdx.x == 0) la.cycles[(int64_t)slice * la.n_items + item] = (int64_t)(clock64() - t0);
     }
 }
 
+template <int NT, int TERMS, bool TIMED, bool PRE>
+int launch_tc4(const LaunchArgs &a, int N, int64_t part_stride, cudaStream_t s) {
+    dim3 grid(a.n_items, (N + NT - 1) / NT);
+    const int smem = TcSmem<NT, PRE>::TOTAL;
+    cudaFuncSetAttribute(spmm_tc_kernel<NT, TERMS, TIMED, PRE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    spmm_tc_kernel<NT, TERMS, TIMED, PRE><<<grid, SABLE_THREADS, smem, s>>>(a, part_stride);
+    return (int)cudaGetLastError();
+}
+
 template <int NT, int TERMS, bool TIMED>
 int launch_tc3(const LaunchArgs &a, int N, int64_t part_stride, cudaStream_t s) {
-    dim3 grid(a.n_items, (N + NT - 1) / NT);
-    const int smem = TcSmem<NT>::TOTAL;
-    cudaFuncSetAttribute(spmm_tc_kernel<NT, TERMS, TIMED>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    spmm_tc_kernel<NT, TERMS, TIMED><<<grid, SABLE_THREADS, smem, s>>>(a, part_stride);
-    return (int)cudaGetLastError();
+    return (a.tcplanes && a.tcoff) ? launch_tc4<NT, TERMS, TIMED, true>(a, N, part_stride, s)
+                                   : launch_tc4<NT, TERMS, TIMED, false>(a, N, part_stride, s);
 }
 
 template <int NT>
@@ -57,6 +69,11 @@ int launch_spmm_tc(const LaunchArgs &a, int N, int nt, int terms, int64_t part_s
     }
 }
 
-void spmm_tc_free(sable_plan *p) { (void)p; }
+void spmm_tc_free(sable_plan *p) {
+    cudaFree(p->d_tcplanes);
+    cudaFree(p->d_tcoff);
+    p->d_tcplanes = nullptr;
+    p->d_tcoff = nullptr;
+}
 
 }  // namespace sable
