@@ -53,6 +53,8 @@ static_assert(sizeof(BatchUnit) == 8, "BatchUnit must stay 8 bytes");
 struct BatchArgs {
     const unsigned char *records;
     const ItemRef *items;
+    const uint4 *tcplanes;  // pre-split A fragments of the plans that have them, merged
+    const int64_t *tcoff;   // per merged item: word offset in tcplanes, -1: split per K step
     const BatchUnit *units;
     const MatIO *mats;
     int *head;           // queue head, zero before each launch
@@ -61,16 +63,30 @@ struct BatchArgs {
     int stage_bytes;     // bytes of one SpMV stage (>= largest SpMV record)
 };
 
-__device__ __forceinline__ void run_spmm_unit(const BatchUnit U, const unsigned char *R, const MatIO &io,
-                                              unsigned char *smem) {
+__device__ __forceinline__ void run_spmm_unit(const BatchArgs &b, const BatchUnit U, const unsigned char *R,
+                                              const MatIO &io, unsigned char *smem) {
+    const int64_t po = (U.kind >= U_TC2_32 && b.tcoff) ? b.tcoff[U.item] : -1;
+    const uint4 *pl = po >= 0 ? b.tcplanes + po : nullptr;
     switch (U.kind) {
         case U_F32_16: spmm_fp32_item<16>(R, io, U.slice, io.part_stride, smem); break;
         case U_F32_32: spmm_fp32_item<32>(R, io, U.slice, io.part_stride, smem); break;
         case U_F32_64: spmm_fp32_item<64>(R, io, U.slice, io.part_stride, smem); break;
-        case U_TC2_32: spmm_tc_item<32, 2>(R, io, U.slice, io.part_stride, smem); break;
-        case U_TC2_64: spmm_tc_item<64, 2>(R, io, U.slice, io.part_stride, smem); break;
-        case U_TC3_32: spmm_tc_item<32, 3>(R, io, U.slice, io.part_stride, smem); break;
-        case U_TC3_64: spmm_tc_item<64, 3>(R, io, U.slice, io.part_stride, smem); break;
+        case U_TC2_32:
+            if (pl) spmm_tc_item<32, 2, true>(R, io, U.slice, io.part_stride, smem, pl);
+            else spmm_tc_item<32, 2>(R, io, U.slice, io.part_stride, smem);
+            break;
+        case U_TC2_64:
+            if (pl) spmm_tc_item<64, 2, true>(R, io, U.slice, io.part_stride, smem, pl);
+            else spmm_tc_item<64, 2>(R, io, U.slice, io.part_stride, smem);
+            break;
+        case U_TC3_32:
+            if (pl) spmm_tc_item<32, 3, true>(R, io, U.slice, io.part_stride, smem, pl);
+            else spmm_tc_item<32, 3>(R, io, U.slice, io.part_stride, smem);
+            break;
+        case U_TC3_64:
+            if (pl) spmm_tc_item<64, 3, true>(R, io, U.slice, io.part_stride, smem, pl);
+            else spmm_tc_item<64, 3>(R, io, U.slice, io.part_stride, smem);
+            break;
         default: break;
     }
 }
@@ -126,7 +142,7 @@ batch_kernel(const BatchArgs b) {
             const ItemRef ref = b.items[U.item];
             const unsigned char *R = b.records + ref.off;
             if (reinterpret_cast<const ItemHeader *>(R)->bytes == ref.bytes) {
-                run_spmm_unit(U, R, b.mats[reinterpret_cast<const ItemHeader *>(R)->mat], smem);
+                run_spmm_unit(b, U, R, b.mats[reinterpret_cast<const ItemHeader *>(R)->mat], smem);
             } else if (tid == CTRL) {
                 atomicExch(b.error, 1);
             }
@@ -195,13 +211,14 @@ int16_t spmm_kind(int nt, int tc_terms) {
     return nt == 32 ? U_TC3_32 : U_TC3_64;
 }
 
-int spmm_unit_smem(int16_t kind) {
+// pre: the unit's A fragments come pre-split (a larger A stage)
+int spmm_unit_smem(int16_t kind, bool pre) {
     switch (kind) {
         case U_F32_16: return SpmmSmem<16>::TOTAL;
         case U_F32_32: return SpmmSmem<32>::TOTAL;
         case U_F32_64: return SpmmSmem<64>::TOTAL;
-        case U_TC2_32: case U_TC3_32: return TcSmem<32>::TOTAL;
-        case U_TC2_64: case U_TC3_64: return TcSmem<64>::TOTAL;
+        case U_TC2_32: case U_TC3_32: return pre ? TcSmem<32, true>::TOTAL : TcSmem<32>::TOTAL;
+        case U_TC2_64: case U_TC3_64: return pre ? TcSmem<64, true>::TOTAL : TcSmem<64>::TOTAL;
         default: return 0;
     }
 }
@@ -229,6 +246,8 @@ struct sable_batch {
     std::vector<int64_t> n_rows, n_cols;
     unsigned char *d_records = nullptr;
     ItemRef *d_items = nullptr;
+    uint4 *d_tcplanes = nullptr;         // merged pre-split A fragments (or nullptr)
+    int64_t *d_tcoff = nullptr;          // per merged item, -1: none
     BatchUnit *d_units = nullptr;
     MatIO *d_mats = nullptr;
     MatIO *h_mats = nullptr;          // pinned staging of the matrix table
@@ -256,6 +275,8 @@ int batch_launch(sable_batch *bt, cudaStream_t s) {
     BatchArgs a;
     a.records = bt->d_records;
     a.items = bt->d_items;
+    a.tcplanes = bt->d_tcplanes;
+    a.tcoff = bt->d_tcplanes ? bt->d_tcoff : nullptr;
     a.units = bt->d_units;
     a.mats = bt->d_mats;
     a.head = bt->d_head;
@@ -298,6 +319,8 @@ int sable_batch_destroy(sable_batch *bt) {
     if (bt->cap_stream) cudaStreamDestroy(bt->cap_stream);
     if (bt->done) cudaEventDestroy(bt->done);
     cudaFree(bt->d_records);
+    cudaFree(bt->d_tcplanes);
+    cudaFree(bt->d_tcoff);
     cudaFree(bt->d_items);
     cudaFree(bt->d_units);
     cudaFree(bt->d_mats);
@@ -350,6 +373,8 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     }
     if (n_items >= INT32_MAX) return bail(fail(SABLE_ERR_UNSUPPORTED, "batch of %lld items", (long long)n_items));
     std::vector<ItemRef> items;
+    std::vector<int64_t> item_tcoff;  // merged pre-split fragment offsets, -1: none
+    int64_t tc_base = 0;
     std::vector<int32_t> item_mat;
     items.reserve(n_items);
     item_mat.reserve(n_items);
@@ -391,6 +416,7 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
             r.off += rec_base;
             const int32_t idx = (int32_t)items.size();
             items.push_back(r);
+            item_tcoff.push_back(terms && !p->tcoff_host.empty() ? tc_base + p->tcoff_host[k] : -1);
             item_mat.push_back(i);
             if (kind == U_SPMV) bt->stage_bytes = std::max(bt->stage_bytes, r.bytes);
             for (int sl = 0; sl < slices; ++sl) {
@@ -409,6 +435,7 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
                 splits.push_back(t);
             }
         rec_base += p->records_bytes;
+        if (terms && !p->tcoff_host.empty()) tc_base += p->tc_words;
     }
     std::stable_sort(q.begin(), q.end(), [](const Sortable &a, const Sortable &b) {
         return a.cls != b.cls ? a.cls < b.cls : a.cost > b.cost;
@@ -417,7 +444,7 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     int spmm_smem = 0;
     for (size_t k = 0; k < q.size(); ++k) {
         units[k] = q[k].u;
-        spmm_smem = std::max(spmm_smem, spmm_unit_smem(q[k].u.kind));
+        spmm_smem = std::max(spmm_smem, spmm_unit_smem(q[k].u.kind, item_tcoff[q[k].u.item] >= 0));
     }
     bt->n_units = (int64_t)units.size();
     if (bt->n_units >= INT32_MAX) return bail(fail(SABLE_ERR_UNSUPPORTED, "batch of %lld units", (long long)bt->n_units));
@@ -461,6 +488,10 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
 
     int64_t &bytes = bt->device_bytes;
     if ((rc = dev_alloc(&bt->d_records, (size_t)rec_total, &bytes, "records"))) return bail(rc);
+    if (tc_base > 0) {
+        if ((rc = dev_alloc(&bt->d_tcplanes, (size_t)tc_base, &bytes, "split-BF16 panels"))) return bail(rc);
+        if ((rc = dev_alloc(&bt->d_tcoff, item_tcoff.size(), &bytes, "split-BF16 offsets"))) return bail(rc);
+    }
     if ((rc = dev_alloc(&bt->d_items, items.size(), &bytes, "items"))) return bail(rc);
     if ((rc = dev_alloc(&bt->d_units, units.size(), &bytes, "units"))) return bail(rc);
     if ((rc = dev_alloc(&bt->d_mats, mats.size(), &bytes, "matrix table"))) return bail(rc);
@@ -480,6 +511,18 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
             e = cudaMemcpy(bt->d_records + rec_base, plans[i]->d_records, (size_t)plans[i]->records_bytes,
                            cudaMemcpyDeviceToDevice);
         rec_base += plans[i]->records_bytes;
+    }
+    if (tc_base > 0) {
+        int64_t wb = 0;
+        for (int i = 0; i < n_plans && e == cudaSuccess; ++i) {
+            const sable_plan *p = plans[i];
+            const bool tc = widths[i] >= 32 && p->spmm_tc && !p->tcoff_host.empty();
+            if (!tc) continue;
+            e = cudaMemcpy(bt->d_tcplanes + wb, p->d_tcplanes, (size_t)p->tc_words * sizeof(uint4), cudaMemcpyDeviceToDevice);
+            wb += p->tc_words;
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpy(bt->d_tcoff, item_tcoff.data(), item_tcoff.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_items, items.data(), items.size() * sizeof(ItemRef), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)

@@ -171,6 +171,8 @@ static int build_tc_planes(sable_plan *p, const Layout &L, int64_t *bytes) {
     int rc = upload_vec(reinterpret_cast<uint32_t **>(&p->d_tcplanes), words.data(), words.size(), "split-BF16 panels",
                         bytes);
     if (rc) return rc;
+    p->tcoff_host = off;
+    p->tc_words = (int64_t)(words.size() / 4);
     return upload_vec(&p->d_tcoff, off.data(), off.size(), "split-BF16 offsets", bytes);
 }
 

@@ -53,6 +53,8 @@ struct sable_plan {
     bool staged_ok = true;               // records fit the shared-memory staging of SpMV and batches
     void *d_tcplanes = nullptr;          // split-BF16 SpMM: pre-split A fragments (16-byte words)
     int64_t *d_tcoff = nullptr;          // word offset of each item's fragments (item-table order)
+    std::vector<int64_t> tcoff_host;     // the same on the host (empty: no fragments)
+    int64_t tc_words = 0;                // 16-byte words in d_tcplanes
     float *d_ppartial = nullptr;         // multi-part tile partials
     int *d_pcounters = nullptr;          // multi-part tile counters
     int64_t n_parts = 0, n_multi = 0;
