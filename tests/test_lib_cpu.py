@@ -114,6 +114,27 @@ def test_layout_builder_edge_shapes(row_tile, chunk_bytes, split_layout, schedul
     assert st["dense_padded"] >= st["dense_values"]
 
 
+@pytest.mark.parametrize("dense_frac", [0.0, 1.0, 0.5])
+@pytest.mark.parametrize("split_layout", [0, 1])
+def test_compact_window_overflow_splits(dense_frac, split_layout):
+    """Compact records: a block row whose panel columns or CSR columns exceed
+    the 1024-position x window is cut into more items until every window
+    fits; the builder's checker (check_compact_layout) passes and nothing is
+    lost."""
+    rng = np.random.default_rng(5)
+    rs, cs = np.array([8, 30]), np.full(60, 40)   # 2400 columns per block row
+    present = np.ones((2, 60), bool)
+    m = synth.assemble(rng, rs, cs, present, lambda r, h, w, a, b: r.uniform(-1, 1, (h, w)) *
+                       (r.random((h, w)) < 0.3))
+    dense = rng.random(m.n_blocks) < dense_frac
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense)
+    st = dry_run(comp, 8, 32768, split_layout, schedule=2)
+    bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+    assert st["dense_values"] == int(bt.size[dense].sum())
+    assert st["sparse_nnz"] == (0 if comp.indptr is None else int(comp.indptr[-1]))
+    assert st["n_chunks"] > st["n_tiles"]   # windows forced splits
+
+
 def test_large_items_schedule_0_only():
     """chunk_bytes above the staging size: accepted for one CTA per item (an
     SpMM-only plan), refused for the warp executors."""
