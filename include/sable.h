@@ -76,7 +76,7 @@ typedef struct sable_plan_opts {
     int32_t row_tile;     /* rows per tile, 1..128 (0: 128; schedule 2 caps
                              tiles at 64 rows)                                 */
     int32_t chunk_bytes;  /* target matrix bytes per work item, 4096..78643
-                             (0: 32768; 8192 for schedule 1, 16384 for 2);
+                             (0: 32768; 8192 for schedule 1);
                              schedule 0 takes up to 1048576: a plan whose
                              items exceed 98304 bytes is an SpMM-only plan
                              (long K loops, no split tiles): SpMV and batches

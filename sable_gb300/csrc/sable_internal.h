@@ -56,7 +56,7 @@
 #define SABLE_SCHEDULE_ITEMS 0
 #define SABLE_SCHEDULE_PERSISTENT 1
 #define SABLE_SCHEDULE_WARP_ITEMS 2
-#define SABLE_WARP_ITEMS_ITEM_BYTES 16384  // default item size, one warp per item
+#define SABLE_WARP_ITEMS_ITEM_BYTES 32768  // default item size, one warp per compact item
 
 struct __align__(16) ItemHeader {
     int32_t row0;       // first output row of the tile
