@@ -7,9 +7,11 @@
 //   spmv_items_kernel  one CTA (8 warps) per item: a single TMA bulk copy
 //                      (cp.async.bulk, completion counted on an mbarrier)
 //                      brings the item's record into shared memory; x values
-//                      are read through L1.  Split tiles are combined by the
-//                      last-arriving CTA.  This is the plain form and the one
-//                      the timed entry points use.
+//                      are read through L1.  Split tiles are combined by a
+//                      separate combine launch.  This is the plain form and
+//                      the one the timed entry points use for schedules 0-1.
+//   spmv_warp_items_kernel  one warp per compact item (schedule 2; described
+//                      with the kernel below), the fastest on large matrices.
 //   spmv_warp_kernel   persistent warp workers: every warp walks its own
 //                      LPT-balanced list of parts (runs of items of one tile)
 //                      through a private 2-slot TMA ring; while item k is
