@@ -23,7 +23,13 @@ def _stream_handle(stream) -> int | None:
 
 
 class Plan:
-    """GPU plan of one compressed VBR matrix."""
+    """GPU plan of one compressed VBR matrix.
+
+    schedule "items" (one CTA per work item) serves SpMV, SpMM and batches;
+    with chunk_bytes above 78643 (up to 1 MB, whole block rows per item) it
+    is an SpMM-only plan.  "warp_items" (one warp per compact work item, the
+    fastest SpMV on large matrices) is an SpMV-only plan.  The other product
+    on such a plan raises SableError (SABLE_ERR_UNSUPPORTED)."""
 
     SCHEDULES = {"items": 0, "persistent": 1, "warp_items": 2}
     SPLIT_LAYOUTS = {"mixed": 0, "separate": 1}
