@@ -37,10 +37,11 @@ from .plan import Plan
 
 # Launch shapes the entry points use unless plan options say otherwise: the
 # fastest shapes measured on large matrices (one warp per 32 KB work item over
-# 16-row tiles for SpMV; one CTA per work item with separate dense and CSR
-# items for SpMM).  sable_gb300.autotune picks per matrix.
+# 16-row tiles for SpMV; one CTA per work item of up to 256 KB, whole block
+# rows, with separate dense and CSR items for SpMM: an SpMM-only plan).
+# sable_gb300.autotune picks per matrix.
 SPMV_SHAPE = {"schedule": "warp_items", "row_tile": 16, "chunk_bytes": 32768}
-SPMM_SHAPE = {"split_layout": "separate"}
+SPMM_SHAPE = {"split_layout": "separate", "row_tile": 128, "chunk_bytes": 262144}
 
 
 def _with(defaults: dict, opts: dict) -> dict:
