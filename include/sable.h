@@ -129,6 +129,16 @@ int sable_plan_get_stats(const sable_plan *plan, sable_plan_stats *out);
  * the device layout, and reports its sizes without touching the GPU. */
 int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts, sable_plan_stats *out);
 
+/* Host-only layout build (no CUDA; no counterpart in the reference, whose
+ * inspector emits C instead): the work-item records exactly as a plan of
+ * these options uploads them, and each item's record offset and bytes in
+ * record order.  With records == NULL only *records_bytes and *n_items are
+ * set; SABLE_ERR_ARG when the buffers are smaller than the layout.  Lets
+ * host code check a layout (the record formats are in sable_internal.h). */
+int sable_plan_layout_host(const sable_vbrc_desc *desc, const sable_plan_opts *opts, unsigned char *records,
+                           int64_t records_cap, int64_t *records_bytes, int64_t *item_off, int32_t *item_bytes,
+                           int64_t items_cap, int64_t *n_items);
+
 /* Executor, SpMV: y = A x (replaces the timed loop of the generated program,
  * src/codegen.py:414-439).  x has n_cols floats, y n_rows floats. */
 int sable_spmv(sable_plan *plan, const float *x_dev, float *y_dev, void *stream);

@@ -67,6 +67,8 @@ SIGNATURES = {
     "sable_plan_destroy": (c_int, [c_void_p]),
     "sable_plan_get_stats": (c_int, [c_void_p, POINTER(PlanStats)]),
     "sable_plan_dry_run": (c_int, [POINTER(VbrcDesc), POINTER(PlanOpts), POINTER(PlanStats)]),
+    "sable_plan_layout_host": (c_int, [POINTER(VbrcDesc), POINTER(PlanOpts), c_void_p, c_int64, POINTER(c_int64),
+                                       c_void_p, c_void_p, c_int64, POINTER(c_int64)]),
     "sable_plan_check": (c_int, [c_void_p, c_void_p]),
     "sable_spmv": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
     "sable_spmv_host": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

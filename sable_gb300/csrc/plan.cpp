@@ -659,8 +659,8 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
     return SABLE_OK;
 }
 
-int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts, sable_plan_stats *out) {
-    if (!out) return fail(SABLE_ERR_ARG, "null output pointer");
+// Option checks and the host layout of sable_plan_create, without CUDA.
+static int host_layout(const sable_vbrc_desc *desc, const sable_plan_opts *opts, Layout &L) {
     const int row_tile = opts && opts->row_tile ? opts->row_tile : SABLE_MAX_ROW_TILE;
     const int chunk_bytes = opts && opts->chunk_bytes ? opts->chunk_bytes
                             : (!opts || opts->schedule == SABLE_SCHEDULE_ITEMS ? SABLE_ITEMS_ITEM_BYTES
@@ -674,9 +674,14 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
     if (rc) return rc;
     const int split_layout = opts ? opts->split_layout : 0;
     if (split_layout != 0 && split_layout != 1) return fail(SABLE_ERR_ARG, "split_layout %d unknown", split_layout);
+    return build_layout(desc, row_tile, chunk_bytes, split_layout, L,
+                        opts && opts->schedule == SABLE_SCHEDULE_WARP_ITEMS);
+}
+
+int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts, sable_plan_stats *out) {
+    if (!out) return fail(SABLE_ERR_ARG, "null output pointer");
     Layout L;
-    rc = build_layout(desc, row_tile, chunk_bytes, split_layout, L,
-                      opts && opts->schedule == SABLE_SCHEDULE_WARP_ITEMS);
+    const int rc = host_layout(desc, opts, L);
     if (rc) return rc;
     memset(out, 0, sizeof *out);
     out->n_tiles = L.n_tiles;
@@ -687,6 +692,27 @@ int sable_plan_dry_run(const sable_vbrc_desc *desc, const sable_plan_opts *opts,
     out->device_bytes = (int64_t)L.records.size() + (int64_t)L.items.size() * (int64_t)sizeof(ItemRef) +
                         (L.n_partial + L.n_split_tiles) * 4;
     out->scratch_floats = L.n_partial;
+    return SABLE_OK;
+}
+
+int sable_plan_layout_host(const sable_vbrc_desc *desc, const sable_plan_opts *opts, unsigned char *records,
+                           int64_t records_cap, int64_t *records_bytes, int64_t *item_off, int32_t *item_bytes,
+                           int64_t items_cap, int64_t *n_items) {
+    if (!records_bytes || !n_items) return fail(SABLE_ERR_ARG, "null output pointer");
+    Layout L;
+    const int rc = host_layout(desc, opts, L);
+    if (rc) return rc;
+    *records_bytes = (int64_t)L.records.size();
+    *n_items = (int64_t)L.items.size();
+    if (!records) return SABLE_OK;
+    if (records_cap < *records_bytes || items_cap < *n_items || !item_off || !item_bytes)
+        return fail(SABLE_ERR_ARG, "output buffers smaller than the layout (%lld bytes, %lld items)",
+                    (long long)*records_bytes, (long long)*n_items);
+    memcpy(records, L.records.data(), L.records.size());
+    for (size_t k = 0; k < L.items.size(); ++k) {
+        item_off[k] = L.items[k].off;
+        item_bytes[k] = L.items[k].bytes;
+    }
     return SABLE_OK;
 }
 
