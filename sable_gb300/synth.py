@@ -19,9 +19,13 @@ follow the same structure with FP32 values and x drawn from U(-1, 1):
                  [2, 256], density U[0.01, 1], uniform / banded /
                  row-clustered, N in {1, 8, 32, 128}.
 Every generator is deterministic in its seed (numpy default_rng).
+
+vbr_matrix_gen is the reference generator's drop-in: same signature, same
+semantics, a .vbr file written, values 1.0 (see its docstring).
 """
 from __future__ import annotations
 
+import random
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -267,3 +271,72 @@ def vector(n: int, seed: int) -> np.ndarray:
 
 def dense_operand(n: int, N: int, seed: int) -> np.ndarray:
     return np.random.default_rng(seed).uniform(-1.0, 1.0, size=(n, N)).astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# Drop-in for the reference's generator
+# ---------------------------------------------------------------------------
+def _sample_splits(n: int, parts: int) -> list[int]:
+    """`parts` positive sizes summing to n: the gaps between parts - 1 cut
+    points drawn without replacement from 1..n-1 (random_splits,
+    synthesize_matrices/vbr_matrices_gen.py:24-34; Python's `random`)."""
+    if n <= 0 or parts <= 0:
+        raise ValueError("Both n and a must be positive integers.")
+    cuts = sorted(random.sample(range(1, n), parts - 1))
+    bounds = [0, *cuts, n]
+    return [bounds[k + 1] - bounds[k] for k in range(parts)]
+
+
+def vbr_matrix_gen(m: int, n: int, partitioning: str, row_split: int, col_split: int, num_dense: int,
+                   perc_dense_zeros: int, num_sparse: int, dense_blocks_only: bool,
+                   vbr_dir: str = "Generated_VBR") -> str:
+    """Synthetic m x n VBR matrix written to <vbr_dir>/<name>.vbr (dense_blocks_only) or
+    <vbr_dir>_Sparse/<name>.vbr; returns <name>.  The reference generator's signature and
+    semantics (synthesize_matrices/vbr_matrices_gen.py:36-113): row_split x col_split
+    partitions, uniform or drawn by random cuts ("nonuniform"); num_dense blocks at random
+    with perc_dense_zeros % of their entries zero, then num_sparse of the remaining blocks
+    with 10 nonzeros each; every nonzero is 1.0.  The draws come from Python's `random`
+    module in the reference's order (partitions, dense blocks, sparse blocks, then the zero
+    positions of every stored block in block order), so a call after random.seed(s)
+    produces the reference's matrix for the same seed."""
+    from .fileio import write_vbr_matrix
+    from .vbr import VBR
+    assert m % row_split == 0 and n % col_split == 0
+    if partitioning == "nonuniform":
+        rsz, csz = _sample_splits(m, row_split), _sample_splits(n, col_split)
+    elif partitioning == "uniform":
+        rsz, csz = [m // row_split] * row_split, [n // col_split] * col_split
+    else:
+        raise ValueError(f"partitioning {partitioning!r}: 'uniform' or 'nonuniform'")
+    rpntr = np.concatenate([[0], np.cumsum(rsz)]).astype(np.int64)
+    cpntr = np.concatenate([[0], np.cumsum(csz)]).astype(np.int64)
+    n_blocks = row_split * col_split
+    dense = random.sample(range(n_blocks), num_dense)
+    dense_set = set(dense)
+    sparse = random.sample([b for b in range(n_blocks) if b not in dense_set], num_sparse)
+    stored = sorted(dense + sparse)
+    nonzeros_in_sparse = 10
+    vals, indx, bindx = [], [0], []
+    bpntrb = np.full(row_split, -1, np.int64)
+    bpntre = np.full(row_split, -1, np.int64)
+    for k, b in enumerate(stored):
+        a, c = divmod(b, col_split)
+        size = int((rpntr[a + 1] - rpntr[a]) * (cpntr[c + 1] - cpntr[c]))
+        n_zero = size * perc_dense_zeros // 100 if b in dense_set else size - nonzeros_in_sparse
+        block = np.ones(size)
+        block[random.sample(range(size), n_zero)] = 0.0
+        vals.append(block)
+        indx.append(indx[-1] + size)
+        bindx.append(c)
+        if bpntrb[a] == -1:
+            bpntrb[a] = k
+        bpntre[a] = k + 1
+    val = np.concatenate(vals) if vals else np.zeros(0)
+    matrix = VBR(val, np.asarray(indx, np.int64), np.asarray(bindx, np.int64), rpntr, cpntr, bpntrb, bpntre)
+    if dense_blocks_only:
+        name = f"Matrix_{m}_{n}_{row_split}_{col_split}_{num_dense}_{perc_dense_zeros}_{partitioning}"
+        write_vbr_matrix(name, matrix, vbr_dir)
+    else:
+        name = f"Matrix_{m}_{n}_{row_split}_{col_split}_{num_dense}_{perc_dense_zeros}_{num_sparse}_{partitioning}"
+        write_vbr_matrix(name, matrix, vbr_dir + "_Sparse")
+    return name

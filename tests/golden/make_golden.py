@@ -18,9 +18,17 @@ Steps (harness shims only, all inside a scratch copy under /tmp):
   6. run the reference's own generator (vbr_spmv_codegen, vbr_spmm_codegen,
      convert_vbr_to_compressed, and its test functions for the example
      matrices), compile the generated C with the reference CFLAGS
-     (src/consts.py:6) and run it under `ulimit -s unlimited`.
+     (src/consts.py:6) and run it under `ulimit -s unlimited`;
+  7. run the reference's synthetic matrix generator (vbr_matrix_gen,
+     synthesize_matrices/vbr_matrices_gen.py:36-113) after random.seed(s)
+     and store the arrays of the .vbr file it writes.
 The fixtures store the reference's inputs (or the seeds that regenerate
 them, with a sha256 of the arrays) and the printed outputs.
+
+    python tests/golden/make_golden.py --generator-only [/root/reference]
+
+adds (or refreshes) only the generator cases of step 7 in the existing
+fixture files.
 """
 from __future__ import annotations
 
@@ -161,6 +169,61 @@ def spmm_case(name, arrays, X, density, fixtures, meta):
     fixtures[name] = {"kind": "spmm", "density": density, "N": N, **meta, "Y": Y}
 
 
+# vbr_matrix_gen cases: (seed, m, n, partitioning, row_split, col_split, num_dense,
+# perc_dense_zeros, num_sparse, dense_blocks_only)
+GEN_CASES = [
+    (11, 60, 60, "uniform", 6, 5, 8, 20, 6, False),
+    (12, 60, 60, "nonuniform", 6, 5, 8, 20, 0, False),   # random partitions: sparse blocks may hold < 10 entries
+    (13, 120, 90, "nonuniform", 8, 6, 12, 0, 0, True),
+    (14, 120, 90, "uniform", 4, 6, 3, 50, 9, False),
+]
+
+
+def generator_cases(fixtures):
+    """Step 7: the reference generator's matrices for GEN_CASES."""
+    import random
+    gen = importlib.import_module("synthesize_matrices.vbr_matrices_gen")
+    fio = importlib.import_module("utils.fileio")
+    out_dir = SCRATCH / "_gen"
+    for case in GEN_CASES:
+        seed, args = case[0], case[1:]
+        random.seed(seed)
+        name = gen.vbr_matrix_gen(*args, vbr_dir=str(out_dir))
+        sub = out_dir if args[-1] else pathlib.Path(str(out_dir) + "_Sparse")
+        arrays = fio.read_vbr(str(sub / (name + ".vbr")))
+        fixtures[f"vbrgen_{seed}"] = {"kind": "arrays", "seed": seed, "args": list(args), "name": name,
+                                      **{k: np.asarray(v) for k, v in zip(
+                                          ("val", "indx", "bindx", "rpntr", "cpntr", "bpntrb", "bpntre"), arrays)}}
+
+
+def write(fixtures):
+    index = {}
+    arrays_out = {}
+    for name, f in fixtures.items():
+        index[name] = {k: v for k, v in f.items() if not isinstance(v, np.ndarray)}
+        for k, v in f.items():
+            if isinstance(v, np.ndarray):
+                arrays_out[f"{name}__{k}"] = v
+    np.savez_compressed(OUT / "golden.npz", **arrays_out)
+    (OUT / "golden.json").write_text(json.dumps(index, indent=1, default=str))
+    print("wrote", OUT / "golden.npz", "cases:", ", ".join(fixtures))
+
+
+def generator_only(ref_root="/root/reference"):
+    """Refresh only the step-7 cases in the existing fixture files."""
+    index = json.loads((OUT / "golden.json").read_text())
+    with np.load(OUT / "golden.npz") as z:
+        stored = {k: z[k] for k in z.files}
+    fixtures = {name: dict(meta) for name, meta in index.items() if not name.startswith("vbrgen_")}
+    for key, v in stored.items():
+        name, field = key.split("__", 1)
+        if name in fixtures:
+            fixtures[name][field] = v
+    prepare(pathlib.Path(ref_root))
+    generator_cases(fixtures)
+    write(fixtures)
+
+
 def main(ref_root="/root/reference"):
     ref_root = pathlib.Path(ref_root)
     from sable_gb300 import synth
@@ -212,18 +275,12 @@ def main(ref_root="/root/reference"):
                 "sha": sha(*s.arrays(), X)}
         spmm_case(f"spmm400_N{N}_d{dens}", (s.val.astype(np.float64), *s.arrays()[1:]), X, dens, fixtures, meta)
 
-    # write
-    index = {}
-    arrays_out = {}
-    for name, f in fixtures.items():
-        index[name] = {k: v for k, v in f.items() if not isinstance(v, np.ndarray)}
-        for k, v in f.items():
-            if isinstance(v, np.ndarray):
-                arrays_out[f"{name}__{k}"] = v
-    np.savez_compressed(OUT / "golden.npz", **arrays_out)
-    (OUT / "golden.json").write_text(json.dumps(index, indent=1, default=str))
-    print("wrote", OUT / "golden.npz", "cases:", ", ".join(fixtures))
+    generator_cases(fixtures)
+    write(fixtures)
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if sys.argv[1:2] == ["--generator-only"]:
+        generator_only(*sys.argv[2:])
+    else:
+        main(*sys.argv[1:])
