@@ -21,6 +21,8 @@ times (ns) and the result.
   vbr_spmv_cuda_codegen     src/codegen.py:1077-1195 (density rule
                             dense_count > density*(h*w)//100, :1158)
   vbr_spmm_cuda_codegen     src/codegen.py:1312-1436
+  only_nonzeros_spmv        src/baseline.py:10-93 (the per-nonzero baseline:
+  only_nonzeros_spmm        src/baseline.py:94-182  every block CSR)
 """
 from __future__ import annotations
 
@@ -236,3 +238,30 @@ def vbr_spmm_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: i
                                              comp.n_rows,
                                              comp.n_cols, 0, {"density": density}))
     return time.time_ns() // 1_000 - t1
+
+
+# -- the reference's per-nonzero baselines (src/baseline.py) --------------------
+def _nonzeros_only(vbr_dir: str, filename: str):
+    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(os.path.join(vbr_dir, filename + ".vbr"))
+    return compress(np.asarray(val, dtype=np.float32), rpntr, cpntr, indx, bindx, bpntrb, bpntre,
+                    np.zeros(len(bindx), dtype=bool))
+
+
+def only_nonzeros_spmv(filename: str, dir_name: str, vbr_dir: str, bench: int = 5, **plan_opts) -> None:
+    """src/baseline.py:10-93: SpMV that touches every stored nonzero once and
+    no zero (the reference emits one FP32 statement per nonzero).  Here a plan
+    with every block in CSR form (the all-sparse choice) is registered as
+    (dir_name, filename); run_spmv executes it."""
+    comp = _nonzeros_only(vbr_dir, filename)
+    _register(dir_name, filename, PlanRecord(Plan(comp, **_with(SPMV_SHAPE, plan_opts)), "spmv", comp.n_rows,
+                                             comp.n_cols, bench, {"vbr_dir": os.path.abspath(vbr_dir),
+                                                                  "baseline": "only_nonzeros"}))
+
+
+def only_nonzeros_spmm(filename: str, dir_name: str, vbr_dir: str, bench: int = 5, **plan_opts) -> None:
+    """src/baseline.py:94-182: the SpMM counterpart (FP32, every block CSR),
+    registered for run_spmm."""
+    comp = _nonzeros_only(vbr_dir, filename)
+    _register(dir_name, filename, PlanRecord(Plan(comp, **_with(SPMM_SHAPE, plan_opts)), "spmm", comp.n_rows,
+                                             comp.n_cols, bench, {"vbr_dir": os.path.abspath(vbr_dir),
+                                                                  "baseline": "only_nonzeros"}))

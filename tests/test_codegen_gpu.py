@@ -47,3 +47,35 @@ def test_spmm_codegen_example(golden, cuda, tmp_path):
     times, Y = codegen.run_spmm(gen_dir, "example", X=np.ones((11, 512), np.float32))
     np.testing.assert_allclose(Y[:, 0], golden.arr("example_canon", "spmm_rows"), rtol=1e-6)
     assert np.all(Y == Y[:, :1])
+
+
+def test_only_nonzeros_baselines(golden, cuda, tmp_path):
+    """The reference's per-nonzero baselines (src/baseline.py) on its example
+    matrix: every block CSR, the canonical SpMV (x = 1) and SpMM (X = ones)
+    outputs; and on a generated matrix against the FP64 oracle."""
+    ex = golden.arrays("example_arrays")
+    vbr_dir, gen_dir = str(tmp_path / "vbr"), str(tmp_path / "gen")
+    os.makedirs(vbr_dir)
+    fileio.write_vbr_matrix("example", VBR(*[a.tolist() for a in ex]), vbr_dir)
+    codegen.only_nonzeros_spmv("example", gen_dir, vbr_dir)
+    rec = codegen.load_plan(gen_dir, "example")
+    assert rec.plan.stats()["dense_values"] == 0
+    _, y = codegen.run_spmv(gen_dir, "example", np.ones(11, np.float32))
+    np.testing.assert_allclose(y, golden.arr("example_canon", "spmv"), rtol=1e-6)
+    codegen.only_nonzeros_spmm("example", gen_dir, vbr_dir)
+    _, Y = codegen.run_spmm(gen_dir, "example", X=np.ones((11, 512), np.float32))
+    np.testing.assert_allclose(Y[:, 0], golden.arr("example_canon", "spmm_rows"), rtol=1e-6)
+    # a generated matrix (the reference generator's drop-in), random x
+    import random
+    random.seed(5)
+    name = synth.vbr_matrix_gen(240, 200, "uniform", 8, 10, 20, 30, 15, False, vbr_dir=vbr_dir)
+    codegen.only_nonzeros_spmv(name, gen_dir, vbr_dir + "_Sparse")
+    x = synth.vector(200, 6)
+    _, y = codegen.run_spmv(gen_dir, name, x)
+    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(os.path.join(vbr_dir + "_Sparse", name + ".vbr"))
+    m = synth.VbrMatrix(np.asarray(val), np.asarray(indx), np.asarray(bindx), np.asarray(rpntr), np.asarray(cpntr),
+                        np.asarray(bpntrb), np.asarray(bpntre))
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, np.zeros(m.n_blocks, bool))
+    y_ref, ya = oracle.spmv_vbrc(comp, x)
+    r = oracle.report(y, y_ref, ya)
+    assert r["pass"], r
