@@ -162,19 +162,23 @@ int sable_spmm(sable_plan *plan, const float *X_dev, int64_t ldx, float *Y_dev, 
 int sable_spmm_host(sable_plan *plan, const float *X_host, float *Y_host, int32_t N, void *stream);
 
 /* SpMM that allocates no memory (no counterpart in the reference).
- * Same result and arguments as sable_spmm on the FP32 path, for callers that
- * cannot let a library allocate device memory during a call: code running
- * while a CUDA graph is being captured, runtimes whose pool allocator owns
- * all device memory, real-time loops that must not block on cudaMalloc.
+ * Same arguments, kernels and result as sable_spmm (split BF16 on the tensor
+ * cores for plans built with spmm_tc at N >= 32, FP32 otherwise), for callers
+ * that cannot let a library allocate device memory during a call: runtimes
+ * whose pool allocator owns all device memory and forbids later cudaMalloc,
+ * and real-time loops that must not block on the driver's allocator.
  * sable_spmm allocates split-tile scratch on its first call at a given width;
  * this entry point uses a fixed scratch array compiled into the library
  * instead (8 MiB of partial sums + 256 KiB of counters, held by every device
  * that loads the library until the process exits) and returns
  * SABLE_ERR_UNSUPPORTED when a plan at width N needs more than that.
  * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress); make that first call before any stream capture.
- * All calls share the one array: calls that may overlap on the GPU (other
- * streams, other host threads) race and must be serialised by the caller. */
+ * (cudaGetSymbolAddress), which also loads the library's device code on that
+ * device if it is not loaded yet and so reserves the array: make that first
+ * call before any stream capture, and before a pool allocator takes the
+ * whole device.  All calls share the one array and each call clears its
+ * counters first: calls that may overlap on the GPU (other streams, other
+ * host threads) race and must be serialised by the caller. */
 int sable_spmm_noalloc(sable_plan *plan, const float *X_dev, int64_t ldx, float *Y_dev, int64_t ldy,
                        int32_t N, void *stream);
 

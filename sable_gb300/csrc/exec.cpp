@@ -222,12 +222,6 @@ static int run_spmv(sable_plan *p, const float *x, float *y, int64_t *cycles, vo
     return SABLE_OK;
 }
 
-static int pick_nt(int N) {
-    int nt = 4;
-    while (nt < N && nt < 128) nt <<= 1;
-    return nt;
-}
-
 static int ensure_spmm_scratch(sable_plan *p, int nt, int n_slices) {
     const int64_t need = std::max<int64_t>(1, p->n_partial * nt * n_slices);
     if (need > p->spmm_partial_cap) {
@@ -264,7 +258,7 @@ static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_
     if (p->compact) return fail(SABLE_ERR_UNSUPPORTED, "a plan of the per-warp SpMV executor (schedule 2) runs SpMV only");
     int rc = set_device(p->device);
     if (rc) return rc;
-    const int nt = pick_nt(N);
+    const int nt = spmm_slice_width(N);
     const int n_slices = (N + nt - 1) / nt;
     rc = ensure_spmm_scratch(p, nt, n_slices);
     if (rc) return rc;
@@ -282,18 +276,24 @@ static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_
     a.mat0.pad = std::max<int32_t>(p->n_split_tiles, 1);  // counters per N-slice
     a.cycles = cycles;
     a.error = p->d_error;
-    a.tcplanes = p->d_tcplanes;
-    a.tcoff = p->d_tcoff;
     a.n_items = (int)p->n_items;
     a.stage_bytes = p->max_item_bytes;
-    const int64_t part_stride = p->n_partial * nt;
-    // dense blocks on the tensor cores (split-BF16) when enabled and N >= 32
-    const bool tc = p->spmm_tc && N >= 32;
-    int e = tc ? launch_spmm_tc(a, N, nt, p->spmm_tc == SABLE_TC_SPLIT3 ? 3 : 2, part_stride, cycles != nullptr, stream)
-               : launch_spmm_fp32(a, N, nt, part_stride, cycles != nullptr, stream);
     (void)n_slices;
+    const int e = launch_spmm_plan(p, a, N, nt, cycles != nullptr, stream);
     if (e) return cuda_fail((cudaError_t)e, "spmm launch");
     return SABLE_OK;
+}
+
+// The SpMM kernel of a plan at width N: dense blocks on the tensor cores
+// (split BF16) when the plan was built with them and N >= 32, else on the
+// FP32 CUDA cores.  `a` carries the operands and the scratch.
+int launch_spmm_plan(const sable_plan *p, LaunchArgs &a, int N, int nt, bool timed, void *stream) {
+    a.tcplanes = p->d_tcplanes;
+    a.tcoff = p->d_tcoff;
+    const int64_t part_stride = p->n_partial * nt;
+    if (p->spmm_tc && N >= 32)
+        return launch_spmm_tc(a, N, nt, p->spmm_tc == SABLE_TC_SPLIT3 ? 3 : 2, part_stride, timed, stream);
+    return launch_spmm_fp32(a, N, nt, part_stride, timed, stream);
 }
 
 static int ensure_host_staging(sable_plan *p, int64_t nx, int64_t ny) {

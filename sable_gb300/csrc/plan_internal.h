@@ -85,4 +85,7 @@ struct sable_plan {
 namespace sable {
 int plan_upload(sable_plan *p, const Layout &L);
 LaunchArgs spmv_args(const sable_plan *p, const float *x, float *y, int64_t *cycles);
+// SpMM launch of a plan at width N (slice width nt); sets the plan's
+// tensor-core operands in `a` and picks the kernel as sable_spmm does.
+int launch_spmm_plan(const sable_plan *p, LaunchArgs &a, int N, int nt, bool timed, void *stream);
 }  // namespace sable

@@ -169,6 +169,15 @@ struct LaunchArgs {
 };
 
 namespace sable {
+// Width of one SpMM N-slice (one CTA per item and slice): the smallest power
+// of two from 4 to 128 that covers N.  The split-tile scratch of an SpMM call
+// holds n_partial * nt floats per slice, so every entry point that sizes that
+// scratch uses this one function.
+inline int spmm_slice_width(int N) {
+    int nt = 4;
+    while (nt < N && nt < 128) nt <<= 1;
+    return nt;
+}
 int launch_spmv_items(const LaunchArgs &a, bool timed, void *stream);
 int launch_spmv_warp_items(const LaunchArgs &a, bool timed, void *stream);
 // y rows of split tiles from their items' partial sums (after the items ran).

@@ -3,13 +3,19 @@
 // sable_spmm keeps the partial sums of split tiles in a scratch buffer that it
 // allocates with cudaMalloc the first time a plan is run at a given width.
 // Some callers cannot let a library allocate device memory during a call:
-// code running while a CUDA graph is being captured (an allocation there
-// fails or breaks the capture), runtimes that hand all device memory to their
-// own pool allocator up front and forbid later cudaMalloc, and real-time or
-// safety-critical loops that must not block on the driver's allocator.
-// sable_spmm_noalloc gives them the same FP32 SpMM kernel with its scratch in
-// a fixed, file-scope device array instead: the library reserves it once per
-// device when the module loads and never allocates on the call path.
+// runtimes that hand all device memory to their own pool allocator up front
+// and forbid later cudaMalloc (the allocation fails, or takes memory the pool
+// counted on), and real-time or safety-critical loops that must not block on
+// the driver's allocator.  sable_spmm_noalloc gives them the same SpMM kernels
+// as sable_spmm (FP32, or split BF16 on the tensor cores when the plan has it
+// and N >= 32) with the scratch in a fixed, file-scope device array instead.
+//
+// When the array is reserved: with CUDA's lazy module loading (the default),
+// a device reserves the array when this library's device code is first
+// loaded on it, which is at the latest the first sable_spmm_noalloc call on
+// that device (its cudaGetSymbolAddress loads the module).  A caller whose
+// pool allocator takes the whole device should make one call (any plan, any
+// width) before the pool is created, so that the array is already reserved.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <mutex>
@@ -72,8 +78,7 @@ extern "C" int sable_spmm_noalloc(sable_plan *p, const float *X_dev, int64_t ldx
     if (p->compact) return fail(SABLE_ERR_UNSUPPORTED, "a plan of the per-warp SpMV executor (schedule 2) runs SpMV only");
     int rc = set_device(p->device);
     if (rc) return rc;
-    int nt = 4;
-    while (nt < N && nt < 128) nt <<= 1;
+    const int nt = spmm_slice_width(N);
     const int n_slices = (N + nt - 1) / nt;
     const int64_t need_partial = p->n_partial * nt * n_slices;
     const int64_t need_counters = (int64_t)std::max<int32_t>(p->n_split_tiles, 1) * n_slices;
@@ -106,7 +111,9 @@ extern "C" int sable_spmm_noalloc(sable_plan *p, const float *X_dev, int64_t ldx
     a.error = p->d_error;
     a.n_items = (int)p->n_items;
     a.stage_bytes = p->max_item_bytes;
-    int err = launch_spmm_fp32(a, N, nt, p->n_partial * nt, false, stream);
+    // the same kernel choice as sable_spmm (split BF16 on the tensor cores for
+    // plans built with them at N >= 32, else FP32)
+    const int err = launch_spmm_plan(p, a, N, nt, false, stream);
     if (err) return cuda_fail((cudaError_t)err, "spmm (fixed scratch) launch");
     return SABLE_OK;
 }
