@@ -103,7 +103,13 @@ typedef struct sable_plan_opts {
                              1: dense items, then CSR items (better for SpMM,
                                 whose CTAs run the two parts one after the
                                 other)                                         */
+    int32_t tc_kernel;    /* split-BF16 SpMM kernel (plans with spmm_tc):
+                             0: tcgen05 MMAs with TMEM accumulators (default);
+                             1: mma.sync (the warp-level tensor-core path)     */
 } sable_plan_opts;
+
+#define SABLE_TC_KERNEL_UMMA    0
+#define SABLE_TC_KERNEL_MMASYNC 1
 
 #define SABLE_TC_OFF    0
 #define SABLE_TC_SPLIT2 1

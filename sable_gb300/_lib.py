@@ -42,7 +42,7 @@ class VbrcDesc(ctypes.Structure):
 
 class PlanOpts(ctypes.Structure):
     _fields_ = [("row_tile", c_int32), ("chunk_bytes", c_int32), ("spmm_tc", c_int32), ("device", c_int32),
-                ("schedule", c_int32), ("split_layout", c_int32)]
+                ("schedule", c_int32), ("split_layout", c_int32), ("tc_kernel", c_int32)]
 
 
 class PlanStats(ctypes.Structure):

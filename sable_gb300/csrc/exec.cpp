@@ -30,6 +30,7 @@ static int upload_vec(T **dptr, const T *h, size_t n, const char *what, int64_t 
 }
 
 static int build_tc_planes(sable_plan *p, const Layout &L, int64_t *bytes);
+static int build_umma_planes(sable_plan *p, const Layout &L, int64_t *bytes);
 
 
 int plan_upload(sable_plan *p, const Layout &L) {
@@ -102,7 +103,12 @@ int plan_upload(sable_plan *p, const Layout &L) {
     p->stats.dense_values = L.dense_values;
     p->stats.dense_padded = L.dense_padded;
     p->stats.sparse_nnz = L.sparse_nnz;
-    if (p->spmm_tc != SABLE_TC_OFF && !L.compact && (rc = build_tc_planes(p, L, &bytes))) return rc;
+    // split-BF16 SpMM: the panel terms of the tcgen05 kernel, and the
+    // m16n8k16 fragments of the mma.sync kernel (also what batches read)
+    if (p->spmm_tc != SABLE_TC_OFF && !L.compact) {
+        if (p->tc_kernel == SABLE_TC_KERNEL_UMMA && (rc = build_umma_planes(p, L, &bytes))) return rc;
+        if ((rc = build_tc_planes(p, L, &bytes))) return rc;
+    }
     p->stats.device_bytes = bytes;
     p->stats.scratch_floats = L.n_partial;
     return SABLE_OK;
@@ -174,6 +180,56 @@ static int build_tc_planes(sable_plan *p, const Layout &L, int64_t *bytes) {
     p->tcoff_host = off;
     p->tc_words = (int64_t)(words.size() / 4);
     return upload_vec(&p->d_tcoff, off.data(), off.size(), "split-BF16 offsets", bytes);
+}
+
+// Split-BF16 SpMM on tcgen05: every item's dense panel split once into three
+// BF16 terms (t_k = bf16(v - t_0 - ... - t_{k-1}), round to nearest even) and
+// laid out as the B operand of the transposed product (umma.cuh, K-major, no
+// swizzle): per K step ks (16 panel columns) and term t, one block of hp x 32
+// bytes (hp = tile rows rounded up to 16) in which element (row n, column k)
+// sits at byte (n & 7) * 16 + (n >> 3) * 256 + (k & 7) * 2 + (k >> 3) * 128;
+// zeros outside the panel.  An item's blocks are contiguous, [ks][t].
+static int build_umma_planes(sable_plan *p, const Layout &L, int64_t *bytes) {
+    constexpr int TERMS = 3;
+    const std::vector<ItemRef> &table = p->items_host;
+    std::vector<int64_t> off(table.size(), -1);
+    int64_t total = 0;
+    for (size_t idx = 0; idx < table.size(); ++idx) {
+        ItemHeader hd;
+        memcpy(&hd, L.records.data() + table[idx].off, sizeof hd);
+        if (hd.nq <= 0) continue;
+        const int64_t hp = (hd.h + 15) & ~15, nks = (4 * (int64_t)hd.nq + 15) / 16;
+        off[idx] = total;
+        total += nks * TERMS * hp * 32;
+    }
+    if (total == 0) return SABLE_OK;
+    std::vector<unsigned char> buf((size_t)total, 0);
+    for (size_t idx = 0; idx < table.size(); ++idx) {
+        if (off[idx] < 0) continue;
+        const unsigned char *R = L.records.data() + table[idx].off;
+        ItemHeader hd;
+        memcpy(&hd, R, sizeof hd);
+        const float *P = reinterpret_cast<const float *>(R + hd.panel_off);
+        const int h = hd.h, ncol = 4 * hd.nq, hp = (h + 15) & ~15;
+        unsigned char *dst = buf.data() + off[idx];
+        for (int c = 0; c < ncol; ++c) {
+            const int ks = c >> 4, k = c & 15;
+            for (int n = 0; n < h; ++n) {
+                float v = P[((int64_t)(c >> 2) * h + n) * 4 + (c & 3)];
+                const int e = (n & 7) * 16 + (n >> 3) * 256 + (k & 7) * 2 + (k >> 3) * 128;
+                for (int t = 0; t < TERMS; ++t) {
+                    const uint16_t b = bf16_rn(v);
+                    v -= bf16_value(b);
+                    memcpy(dst + ((int64_t)ks * TERMS + t) * hp * 32 + e, &b, 2);
+                }
+            }
+        }
+    }
+    int rc = upload_vec(&p->d_umma, buf.data(), buf.size(), "split-BF16 panel terms", bytes);
+    if (rc) return rc;
+    p->umma_off_host = off;
+    p->umma_bytes = total;
+    return upload_vec(&p->d_umma_off, off.data(), off.size(), "split-BF16 term offsets", bytes);
 }
 
 LaunchArgs spmv_args(const sable_plan *p, const float *x, float *y, int64_t *cycles) {
@@ -290,9 +346,15 @@ static int run_spmm(sable_plan *p, const float *X, int64_t ldx, float *Y, int64_
 int launch_spmm_plan(const sable_plan *p, LaunchArgs &a, int N, int nt, bool timed, void *stream) {
     a.tcplanes = p->d_tcplanes;
     a.tcoff = p->d_tcoff;
+    a.umma = p->d_umma;
+    a.umma_off = p->d_umma_off;
     const int64_t part_stride = p->n_partial * nt;
-    if (p->spmm_tc && N >= 32)
-        return launch_spmm_tc(a, N, nt, p->spmm_tc == SABLE_TC_SPLIT3 ? 3 : 2, part_stride, timed, stream);
+    if (p->spmm_tc && N >= 32) {
+        const int terms = p->spmm_tc == SABLE_TC_SPLIT3 ? 3 : 2;
+        if (p->tc_kernel == SABLE_TC_KERNEL_UMMA && p->d_umma)
+            return launch_spmm_umma(a, N, nt, terms, part_stride, timed, stream);
+        return launch_spmm_tc(a, N, nt, terms, part_stride, timed, stream);
+    }
     return launch_spmm_fp32(a, N, nt, part_stride, timed, stream);
 }
 
@@ -342,6 +404,8 @@ int sable_plan_destroy(sable_plan *p) {
     cudaFree(p->d_x);
     cudaFree(p->d_y);
     spmm_tc_free(p);
+    cudaFree(p->d_umma);
+    cudaFree(p->d_umma_off);
     if (prev >= 0) cudaSetDevice(prev);
     delete p;
     return SABLE_OK;

@@ -646,6 +646,11 @@ int sable_plan_create(const sable_vbrc_desc *desc, const sable_plan_opts *opts, 
         return fail(SABLE_ERR_ARG, "spmm_tc %d unknown", o.spmm_tc);
     }
     p->spmm_tc = o.spmm_tc;
+    if (o.tc_kernel != SABLE_TC_KERNEL_UMMA && o.tc_kernel != SABLE_TC_KERNEL_MMASYNC) {
+        delete p;
+        return fail(SABLE_ERR_ARG, "tc_kernel %d unknown", o.tc_kernel);
+    }
+    p->tc_kernel = o.tc_kernel;
     Layout L;
     if (o.split_layout != 0 && o.split_layout != 1) {
         delete p;

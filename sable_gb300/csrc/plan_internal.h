@@ -55,6 +55,11 @@ struct sable_plan {
     int64_t *d_tcoff = nullptr;          // word offset of each item's fragments (item-table order)
     std::vector<int64_t> tcoff_host;     // the same on the host (empty: no fragments)
     int64_t tc_words = 0;                // 16-byte words in d_tcplanes
+    int tc_kernel = 0;                   // SABLE_TC_KERNEL_UMMA or SABLE_TC_KERNEL_MMASYNC
+    unsigned char *d_umma = nullptr;     // split-BF16 SpMM on tcgen05: panel terms, UMMA K-major layout
+    int64_t *d_umma_off = nullptr;       // byte offset of each item's terms (item-table order), -1: none
+    std::vector<int64_t> umma_off_host;  // the same on the host
+    int64_t umma_bytes = 0;
     float *d_ppartial = nullptr;         // multi-part tile partials
     int *d_pcounters = nullptr;          // multi-part tile counters
     int64_t n_parts = 0, n_multi = 0;

@@ -162,6 +162,8 @@ struct LaunchArgs {
     int64_t *cycles;        // per-item SM cycles (timed variant) or nullptr
     const void *tcplanes;   // SpMM split-BF16: pre-split A fragments (uint4 words) or nullptr
     const int64_t *tcoff;   // word offset of each item's fragments in tcplanes (item-table order)
+    const unsigned char *umma;    // SpMM split-BF16 on tcgen05: panel terms in the UMMA K-major layout
+    const int64_t *umma_off;      // byte offset of each item's terms in umma (item-table order), -1: none
     int *error;             // set to 1 when a bounded device wait runs out
     int n_items;
     int stage_bytes;        // TMA staging bytes per stage (>= largest record)
@@ -191,5 +193,7 @@ int spmv_warp_workers_per_sm(int stage_bytes, int xg_floats);
 int launch_spmm_fp32(const LaunchArgs &a, int N, int nt, int64_t part_stride, bool timed, void *stream);
 // terms = 2: three BF16 products (hi+lo split); 3: six products (hi+mid+lo).
 int launch_spmm_tc(const LaunchArgs &a, int N, int nt, int terms, int64_t part_stride, bool timed, void *stream);
+// The same product on the tcgen05 tensor cores (TMEM accumulators); nt 32..128.
+int launch_spmm_umma(const LaunchArgs &a, int N, int nt, int terms, int64_t part_stride, bool timed, void *stream);
 const char *cuda_error_string(int err);
 }  // namespace sable

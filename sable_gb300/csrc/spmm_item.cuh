@@ -336,6 +336,97 @@ struct TcSmem {
     static constexpr int TOTAL = OFF_RST + RST;
 };
 
+// The end of a (tile item, N-slice) unit shared by the split-BF16 kernels:
+// adds the item's CSR entries (FP32, CUDA cores; warps own row ranges of
+// about ns/8 entries, lane subgroups combined by xor shuffles once per row)
+// into the Y tile in shared memory, then stores the tile: directly for a
+// single-item tile, else as a partial tile, the last-arriving CTA of the tile
+// summing the partials in item order.  On entry every row < h of the Y tile
+// (row-major h x NT floats at ys4) holds the dense part.
+template <int NT>
+__device__ __forceinline__ void spmm_tile_finish(const unsigned char *R, const ItemHeader &c, const MatIO &a,
+                                                 int slice, int64_t part_stride, float4 *ys4, int *rst) {
+    constexpr int CQ = NT / 4;
+    constexpr int RSUB = 32 / CQ;
+    __shared__ int s_last;
+    __shared__ int s_wrow[9];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int cq = lane % CQ, rs = lane / CQ;
+    const int h = c.h, n0 = slice * NT;
+    const float *__restrict__ X = a.x;
+    // ---- CSR entries (FP32, CUDA cores) ----------------------------------------
+    const bool col_ok = (n0 + 4 * cq) < a.N;
+    __syncthreads();
+    if (c.ns > 0) {
+        const uint2 *__restrict__ E = reinterpret_cast<const uint2 *>(R + c.csr_off);
+        const int ns = c.ns;
+        for (int i = tid; i <= h; i += SABLE_THREADS) rst[i] = __ldg(reinterpret_cast<const int *>(R + c.rp_off) + i);
+        __syncthreads();
+        if (warp == 0 && lane < 9) {
+            const int target = (int)(((int64_t)ns * lane) / 8);
+            int lo = 0, hi = h;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (rst[mid] >= target) hi = mid; else lo = mid + 1;
+            }
+            s_wrow[lane] = lane == 8 ? h : lo;
+        }
+        __syncthreads();
+        for (int r = s_wrow[warp]; r < s_wrow[warp + 1]; ++r) {
+            const int b = rst[r], e = rst[r + 1];
+            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int base = b; base < e; base += RSUB) {
+                const int i = base + rs;
+                if (i < e && col_ok) {
+                    const uint2 en = __ldg(E + i);
+                    s = fma4(__uint_as_float(en.x),
+                             __ldg(reinterpret_cast<const float4 *>(X + (int64_t)en.y * a.ldx + n0 + 4 * cq)), s);
+                }
+            }
+#pragma unroll
+            for (int o = CQ; o < 32; o <<= 1) {
+                s.x += __shfl_xor_sync(FULL, s.x, o);
+                s.y += __shfl_xor_sync(FULL, s.y, o);
+                s.z += __shfl_xor_sync(FULL, s.z, o);
+                s.w += __shfl_xor_sync(FULL, s.w, o);
+            }
+            if (rs == 0 && e > b) ys4[r * CQ + cq] = add4(ys4[r * CQ + cq], s);
+        }
+    }
+    __syncthreads();
+
+    // ---- output -------------------------------------------------------------------
+    const bool split = c.nitem > 1;
+    const int64_t pbase = (int64_t)slice * part_stride + (c.part_base + (int64_t)c.kidx * h) * NT;
+    for (int e = tid; e < h * CQ; e += SABLE_THREADS) {
+        const int i = e / CQ, q = e - i * CQ, n = n0 + 4 * q;
+        if (n >= a.N) continue;
+        const float4 v = ys4[i * CQ + q];
+        if (!split) *reinterpret_cast<float4 *>(a.y + (int64_t)(c.row0 + i) * a.ldy + n) = v;
+        else *reinterpret_cast<float4 *>(a.partial + pbase + (int64_t)i * NT + 4 * q) = v;
+    }
+    if (split) {
+        // split-K arrival as in cta_finish: barrier, one gpu-scope acq_rel
+        // arrival, barrier; the last CTA reads the partials through L2
+        __syncthreads();
+        int *cnt = a.counters + (int64_t)slice * a.pad + c.tile;
+        if (tid == 0) s_last = (arrive_acq_rel(cnt) == c.nitem - 1);
+        __syncthreads();
+        if (s_last) {
+            const int64_t tb = (int64_t)slice * part_stride + c.part_base * NT;
+            for (int e = tid; e < h * CQ; e += SABLE_THREADS) {
+                const int i = e / CQ, q = e - i * CQ, n = n0 + 4 * q;
+                if (n >= a.N) continue;
+                float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int k = 0; k < c.nitem; ++k)
+                    s = add4(s, __ldcg(reinterpret_cast<const float4 *>(a.partial + tb + ((int64_t)k * h + i) * NT + 4 * q)));
+                *reinterpret_cast<float4 *>(a.y + (int64_t)(c.row0 + i) * a.ldy + n) = s;
+            }
+            if (tid == 0) *cnt = 0;
+        }
+    }
+}
+
 // PRE: the item's A fragments come pre-split (planes: the item's words, see
 // stage_tc_planes) instead of being split from the FP32 panel on every step.
 template <int NT, int TERMS, bool PRE = false>
@@ -349,14 +440,11 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
     constexpr int WM = 8 / WN;                            // warps along M
     constexpr int NPW = (NTILES + WN - 1) / WN;           // N-tiles per warp
     constexpr int MPW = (SABLE_MAX_ROW_TILE / 16 + WM - 1) / WM;  // M-tiles per warp (max)
-    constexpr int RSUB = 32 / CQ;
     float *ys = reinterpret_cast<float *>(smem);
     float4 *ys4 = reinterpret_cast<float4 *>(smem);
     float *Bs = reinterpret_cast<float *>(smem + L::OFF_BS);
     float4 *As = reinterpret_cast<float4 *>(smem + L::OFF_AS);
     int *rst = reinterpret_cast<int *>(smem + L::OFF_RST);
-    __shared__ int s_last;
-    __shared__ int s_wrow[9];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int g = lane >> 2, t = lane & 3;                 // MMA fragment coordinates
@@ -505,78 +593,7 @@ __device__ __forceinline__ void spmm_tc_item(const unsigned char *R, const MatIO
         }
     }
 
-    // ---- CSR entries (FP32, CUDA cores) ----------------------------------------
-    const int cq = lane % CQ, rs = lane / CQ;
-    const bool col_ok = (n0 + 4 * cq) < a.N;
-    __syncthreads();
-    if (c.ns > 0) {
-        const uint2 *__restrict__ E = reinterpret_cast<const uint2 *>(R + c.csr_off);
-        const int ns = c.ns;
-        for (int i = tid; i <= h; i += SABLE_THREADS) rst[i] = __ldg(reinterpret_cast<const int *>(R + c.rp_off) + i);
-        __syncthreads();
-        if (warp == 0 && lane < 9) {
-            const int target = (int)(((int64_t)ns * lane) / 8);
-            int lo = 0, hi = h;
-            while (lo < hi) {
-                const int mid = (lo + hi) >> 1;
-                if (rst[mid] >= target) hi = mid; else lo = mid + 1;
-            }
-            s_wrow[lane] = lane == 8 ? h : lo;
-        }
-        __syncthreads();
-        for (int r = s_wrow[warp]; r < s_wrow[warp + 1]; ++r) {
-            const int b = rst[r], e = rst[r + 1];
-            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int base = b; base < e; base += RSUB) {
-                const int i = base + rs;
-                if (i < e && col_ok) {
-                    const uint2 en = __ldg(E + i);
-                    s = fma4(__uint_as_float(en.x),
-                             __ldg(reinterpret_cast<const float4 *>(X + (int64_t)en.y * a.ldx + n0 + 4 * cq)), s);
-                }
-            }
-#pragma unroll
-            for (int o = CQ; o < 32; o <<= 1) {
-                s.x += __shfl_xor_sync(FULL, s.x, o);
-                s.y += __shfl_xor_sync(FULL, s.y, o);
-                s.z += __shfl_xor_sync(FULL, s.z, o);
-                s.w += __shfl_xor_sync(FULL, s.w, o);
-            }
-            if (rs == 0 && e > b) ys4[r * CQ + cq] = add4(ys4[r * CQ + cq], s);
-        }
-    }
-    __syncthreads();
-
-    // ---- output -------------------------------------------------------------------
-    const bool split = c.nitem > 1;
-    const int64_t pbase = (int64_t)slice * part_stride + (c.part_base + (int64_t)c.kidx * h) * NT;
-    for (int e = tid; e < h * CQ; e += SABLE_THREADS) {
-        const int i = e / CQ, q = e - i * CQ, n = n0 + 4 * q;
-        if (n >= a.N) continue;
-        const float4 v = ys4[i * CQ + q];
-        if (!split) *reinterpret_cast<float4 *>(a.y + (int64_t)(c.row0 + i) * a.ldy + n) = v;
-        else *reinterpret_cast<float4 *>(a.partial + pbase + (int64_t)i * NT + 4 * q) = v;
-    }
-    if (split) {
-        // split-K arrival as in cta_finish: barrier, one gpu-scope acq_rel
-        // arrival, barrier; the last CTA reads the partials through L2
-        __syncthreads();
-        int *cnt = a.counters + (int64_t)slice * a.pad + c.tile;
-        if (tid == 0) s_last = (arrive_acq_rel(cnt) == c.nitem - 1);
-        __syncthreads();
-        if (s_last) {
-            const int64_t tb = (int64_t)slice * part_stride + c.part_base * NT;
-            for (int e = tid; e < h * CQ; e += SABLE_THREADS) {
-                const int i = e / CQ, q = e - i * CQ, n = n0 + 4 * q;
-                if (n >= a.N) continue;
-                float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-                for (int k = 0; k < c.nitem; ++k)
-                    s = add4(s, __ldcg(reinterpret_cast<const float4 *>(a.partial + tb + ((int64_t)k * h + i) * NT + 4 * q)));
-                *reinterpret_cast<float4 *>(a.y + (int64_t)(c.row0 + i) * a.ldy + n) = s;
-            }
-            if (tid == 0) *cnt = 0;
-        }
-    }
+    spmm_tile_finish<NT>(R, c, a, slice, part_stride, ys4, rst);
 }
 
 }  // namespace

@@ -1,0 +1,257 @@
+// Split-BF16 SpMM of one (item record, N-slice) unit on the tcgen05 tensor
+// cores, by one CTA of SABLE_THREADS threads.  Replaces the dense-block part
+// of gen_single_threaded_spmm (src/codegen.py:827-937; spmm_kernel, :851-859)
+// for plans built with spmm_tc and N >= 32; the CSR entries of the item stay
+// FP32 on the CUDA cores (spmm_tile_finish).
+//
+// The product is computed transposed, so that the SpMM width fills the
+// 128-row MMA:   D[m][n] = sum_k X[col(k)][n0 + m] * A[row0 + n][col(k)]
+//   m  column of Y within the N-slice (M = 128 TMEM lanes; lanes >= NT unused)
+//   n  row of the item's tile (the MMA's N = h rounded up to 16, <= 128)
+//   k  panel column of the item (K steps of 16; col(k) = the record's xcol)
+// Both operands are split into BF16 terms by repeated round-to-nearest (see
+// spmm_item.cuh), and TERMS = 3 (six products) or 2 (three products) term
+// products accumulate in FP32 in TMEM.
+//
+// Per K step ks (16 panel columns):
+//   B operand  the tile's panel terms, split once on the host when the plan
+//              is built, in the UMMA K-major layout (umma.cuh): per step 3
+//              blocks of hp x 32 bytes (hp = h rounded up to 16); one bulk
+//              copy (cp.async.bulk, mbarrier completion) brings TERMS of them
+//              into a ring of BST stages, BST - 2 steps ahead of the MMAs.
+//   A operand  the 16 X rows of the step (NT floats each, from L2), loaded
+//              one step ahead into registers with 16-byte loads, split into
+//              TERMS BF16 terms by the CTA and stored in the MN-major layout
+//              (8-byte stores, conflict-free) into a ring of 2 stages.
+//   MMA        thread 0 waits for the step's panel copy, issues the TERMS
+//              products (tcgen05.mma.cta_group::1.kind::f16, M = 128, N = hp,
+//              K = 16) and commits them to the step parity's mbarrier; the
+//              CTA waits for the products of step ks - 2 before it reuses
+//              their stages.
+// After the last step the accumulator is read with tcgen05.ld into the Y
+// tile in shared memory (lane m, column n -> Y[n][m]); TMEM is freed on every
+// path.  Every wait is bounded (WAIT_NS); on expiry the error flag is set, the
+// CTA stops issuing work, waits (bounded) for what it issued and frees TMEM.
+#pragma once
+#include "spmm_item.cuh"
+#include "umma.cuh"
+
+namespace {
+
+constexpr int UMMA_BST = 4;                 // panel-term stages (bulk-copy ring)
+constexpr int UMMA_LOOK = UMMA_BST - 2;     // panel copies issued this many steps ahead
+constexpr int UMMA_M = 128;                 // MMA rows (TMEM lanes)
+constexpr int UMMA_STEP_BLOCK = SABLE_MAX_ROW_TILE * 32;  // bytes of one term block of a step (hp <= 128)
+
+template <int NT, int TERMS>
+struct UmmaSmem {
+    static constexpr int A_STAGE = TERMS * UMMA_M * 32;       // X terms of one step (MN-major, 128 rows)
+    static constexpr int B_STAGE = TERMS * UMMA_STEP_BLOCK;   // panel terms of one step
+    static constexpr int OFF_A = 0;                           // 2 stages
+    static constexpr int OFF_B = OFF_A + 2 * A_STAGE;         // UMMA_BST stages
+    static constexpr int LOOP = OFF_B + UMMA_BST * B_STAGE;
+    static constexpr int YS = SABLE_MAX_ROW_TILE * NT * 4;    // Y tile (after the K loop, over the stages)
+    static constexpr int OFF_RST = (YS > LOOP ? YS : LOOP);
+    static constexpr int TOTAL = OFF_RST + (SABLE_MAX_ROW_TILE + 8) * 4;
+};
+
+// Split four FP32 values into TERMS BF16 terms; t[k] packs the four k-th
+// terms (first value in the low half of t[k].x).
+template <int TERMS>
+__device__ __forceinline__ void split4(const float4 v, uint2 (&t)[TERMS]) {
+    float r0 = v.x, r1 = v.y, r2 = v.z, r3 = v.w;
+#pragma unroll
+    for (int k = 0; k < TERMS; ++k) {
+        const __nv_bfloat16 b0 = __float2bfloat16_rn(r0), b1 = __float2bfloat16_rn(r1);
+        const __nv_bfloat16 b2 = __float2bfloat16_rn(r2), b3 = __float2bfloat16_rn(r3);
+        t[k] = make_uint2(pack2(b0, b1), pack2(b2, b3));
+        r0 -= __bfloat162float(b0);
+        r1 -= __bfloat162float(b1);
+        r2 -= __bfloat162float(b2);
+        r3 -= __bfloat162float(b3);
+    }
+}
+
+// Unit u of a step's X gather (4 NT units of one float4): lane bits pick
+// (k & 7) and the low bits of the M quad so that a warp's 8-byte term stores
+// cover 256 contiguous bytes of the MN-major block (no bank conflicts).
+__device__ __forceinline__ void umma_unit(int u, int &k, int &q) {
+    k = ((u >> 1) & 7) | (((u >> 5) & 1) << 3);
+    q = (u & 1) | (((u >> 4) & 1) << 1) | ((u >> 6) << 2);
+}
+
+// planes: the item's panel terms (3 term blocks of hp x 32 bytes per step).
+template <int NT, int TERMS>
+__device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const MatIO &a, int slice, int64_t part_stride,
+                                               unsigned char *smem, const unsigned char *planes, int *error) {
+    using L = UmmaSmem<NT, TERMS>;
+    constexpr int UNITS = 4 * NT;                                    // float4 loads per step
+    constexpr int UPT = (UNITS + SABLE_THREADS - 1) / SABLE_THREADS; // per thread
+    constexpr int NPROD = TERMS == 3 ? 6 : 3;
+    __shared__ __align__(8) uint64_t s_full[UMMA_BST];   // panel copy of a stage landed
+    __shared__ __align__(8) uint64_t s_done[2];          // products of steps of that parity completed
+    __shared__ uint32_t s_taddr;
+    // abort flags: [ks & 1] is written before and read after the barrier of
+    // step ks (a thread already in step ks + 1 writes the other one), [2]
+    // after the K loop
+    __shared__ int s_abort[3];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const ItemHeader c = *reinterpret_cast<const ItemHeader *>(R);
+    const int h = c.h, nq = c.nq, ncol = 4 * nq;
+    const int n0 = slice * NT;
+    float *ys = reinterpret_cast<float *>(smem);
+    float4 *ys4 = reinterpret_cast<float4 *>(smem);
+    int *rst = reinterpret_cast<int *>(smem + L::OFF_RST);
+
+    if (nq > 0) {
+        const int nks = (ncol + 15) >> 4;
+        const int hp = (h + 15) & ~15;
+        const uint32_t ncols = umma_tmem_cols(hp);
+        const uint32_t step_src = 3u * (uint32_t)hp * 32u;           // bytes of a step in `planes`
+        const uint32_t copy_bytes = (uint32_t)TERMS * (uint32_t)hp * 32u;
+        const uint32_t a_base = smem_addr(smem + L::OFF_A), b_base = smem_addr(smem + L::OFF_B);
+        const uint32_t idesc = umma_idesc_bf16(UMMA_M, hp, true);
+        const int *colmap = reinterpret_cast<const int *>(R + c.xcol_off);
+        const float *__restrict__ X = a.x;
+        if (tid == 0) {
+            for (int s = 0; s < UMMA_BST; ++s) mbar_init(smem_addr(&s_full[s]));
+            mbar_init(smem_addr(&s_done[0]));
+            mbar_init(smem_addr(&s_done[1]));
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            s_abort[0] = s_abort[1] = s_abort[2] = 0;
+        }
+        if (warp == 0) tmem_alloc(smem_addr(&s_taddr), ncols);
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        const uint32_t taddr = s_taddr;
+        // panel copies of the first UMMA_LOOK steps
+        if (tid == 0)
+            for (int j = 0; j < UMMA_LOOK && j < nks; ++j)
+                tma_record(smem_addr(&s_full[j]), smem + L::OFF_B + j * L::B_STAGE, planes + (size_t)j * step_src,
+                           copy_bytes);
+        // X rows of step 0 into registers
+        float4 xr[UPT];
+        auto load_step = [&](int ks) {
+#pragma unroll
+            for (int i = 0; i < UPT; ++i) {
+                const int u = tid + i * SABLE_THREADS;
+                int k, q;
+                umma_unit(u, k, q);
+                const int col = 16 * ks + k, n = n0 + 4 * q;
+                xr[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (u < UNITS && col < ncol && n < a.N)
+                    xr[i] = __ldg(reinterpret_cast<const float4 *>(X + (int64_t)__ldg(colmap + col) * a.ldx + n));
+            }
+        };
+        load_step(0);
+        bool bad = false;       // thread 0: a panel copy wait ran out (published before the next barrier)
+        int issued = UMMA_LOOK < nks ? UMMA_LOOK : nks, landed = 0;   // thread 0: panel copies
+        int steps_run = nks;    // steps whose products were committed (uniform across the CTA)
+        for (int ks = 0; ks < nks; ++ks) {
+            // the products of step ks - 2 have read their A stage (ks & 1) and
+            // their panel stage ((ks + UMMA_LOOK) % UMMA_BST)
+            if (ks >= 2 && !mbar_wait(smem_addr(&s_done[ks & 1]), (uint32_t)(((ks - 2) >> 1) & 1))) s_abort[ks & 1] = 1;
+            if (tid == 0) {
+                if (bad) s_abort[ks & 1] = 1;
+                const int j = ks + UMMA_LOOK;
+                if (j < nks) {
+                    tma_record(smem_addr(&s_full[j % UMMA_BST]), smem + L::OFF_B + (j % UMMA_BST) * L::B_STAGE,
+                               planes + (size_t)j * step_src, copy_bytes);
+                    issued = j + 1;
+                }
+            }
+            float4 cur[UPT];
+#pragma unroll
+            for (int i = 0; i < UPT; ++i) cur[i] = xr[i];
+            if (ks + 1 < nks) load_step(ks + 1);
+            unsigned char *As = smem + L::OFF_A + (ks & 1) * L::A_STAGE;
+#pragma unroll
+            for (int i = 0; i < UPT; ++i) {
+                const int u = tid + i * SABLE_THREADS;
+                if (u < UNITS) {
+                    int k, q;
+                    umma_unit(u, k, q);
+                    uint2 t[TERMS];
+                    split4<TERMS>(cur[i], t);
+                    const int off = umma_mnmajor_off(4 * q, k);
+#pragma unroll
+                    for (int e = 0; e < TERMS; ++e) *reinterpret_cast<uint2 *>(As + e * (UMMA_M * 32) + off) = t[e];
+                }
+            }
+            fence_async_smem();
+            __syncthreads();
+            if (s_abort[ks & 1]) {
+                steps_run = ks;
+                break;
+            }
+            if (tid == 0) {
+                const int s = ks % UMMA_BST;
+                if (mbar_wait(smem_addr(&s_full[s]), (uint32_t)((ks / UMMA_BST) & 1))) {
+                    landed = ks + 1;
+                    tc_fence_after();
+                    const uint32_t a_st = a_base + (uint32_t)((ks & 1) * L::A_STAGE);
+                    const uint32_t b_st = b_base + (uint32_t)(s * L::B_STAGE);
+                    // products (x term, panel term), smallest first
+                    constexpr int PA[6] = {1, 0, 2, 0, 1, 0}, PB[6] = {1, 2, 0, 1, 0, 0};
+                    constexpr int QA[3] = {0, 1, 0}, QB[3] = {1, 0, 0};
+#pragma unroll
+                    for (int p = 0; p < NPROD; ++p) {
+                        const int ta = TERMS == 3 ? PA[p] : QA[p], tb = TERMS == 3 ? PB[p] : QB[p];
+                        const uint64_t ad = umma_sdesc(a_st + (uint32_t)(ta * UMMA_M * 32), UMMA_MN_LBO, UMMA_MN_SBO);
+                        const uint64_t bd = umma_sdesc(b_st + (uint32_t)(tb * hp * 32), UMMA_KM_LBO, UMMA_KM_SBO);
+                        umma_bf16(taddr, ad, bd, idesc, (ks > 0 || p > 0) ? 1u : 0u);
+                    }
+                } else {
+                    bad = true;
+                }
+                umma_commit(smem_addr(&s_done[ks & 1]));
+            }
+        }
+        // Every product issued has completed before TMEM is read or freed:
+        // a commit tracks the MMAs issued since the previous commit, and the
+        // MMAs of one accumulator complete in issue order, so the last step's
+        // commit covers them all.  Every panel copy issued has landed before
+        // the CTA exits.
+        if (tid == 0) {
+            if (bad) s_abort[2] = 1;
+            for (int j = landed; j < issued; ++j)
+                if (!mbar_wait(smem_addr(&s_full[j % UMMA_BST]), (uint32_t)((j / UMMA_BST) & 1))) s_abort[2] = 1;
+        }
+        if (steps_run > 0) {
+            const int last = steps_run - 1;
+            if (!mbar_wait(smem_addr(&s_done[last & 1]), (uint32_t)((last >> 1) & 1))) s_abort[2] = 1;
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (s_abort[0] | s_abort[1] | s_abort[2]) {
+            if (tid == 0) atomicExch(error, 1);
+        } else {
+            // lane m of quadrant (warp & 3) -> Y column n0 + m; the two warp
+            // halves take alternate 16-column chunks of the accumulator
+            const int quad = warp & 3, m = 32 * quad + lane;
+            if (32 * quad < NT) {
+                for (int c0 = 16 * (warp >> 2); c0 < hp; c0 += 32) {
+                    uint32_t r[16];
+                    tmem_ld16(taddr + ((uint32_t)(32 * quad) << 16) + (uint32_t)c0, r);
+#pragma unroll
+                    for (int jj = 0; jj < 16; ++jj)
+                        if (c0 + jj < h) ys[(c0 + jj) * NT + m] = __uint_as_float(r[jj]);
+                }
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (warp == 0) {
+            tc_fence_after();
+            tmem_free(taddr, ncols);
+        }
+    } else {
+        for (int e = tid; e < h * (NT / 4); e += SABLE_THREADS) ys4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    spmm_tile_finish<NT>(R, c, a, slice, part_stride, ys4, rst);
+}
+
+}  // namespace

@@ -37,14 +37,21 @@ class Plan:
     # the tensor cores with 2 terms (3 products) or 3 terms (6 products)
     TC_MODES = {False: 0, True: 1, 0: 0, 1: 1, 2: 2, "off": 0, "split2": 1, "split3": 2}
 
+    # split-BF16 SpMM kernel: tcgen05 MMAs with TMEM accumulators, or the
+    # warp-level mma.sync path
+    TC_KERNELS = {"umma": 0, "mma_sync": 1}
+
     def __init__(self, comp: Compressed, row_tile: int = 0, chunk_bytes: int = 0, spmm_tc=False,
-                 device: int | None = None, schedule: str = "items", split_layout: str = "mixed"):
+                 device: int | None = None, schedule: str = "items", split_layout: str = "mixed",
+                 tc_kernel: str = "umma"):
         lib = _lib.load()
         desc, keep = _lib.make_desc(comp)
         if spmm_tc not in self.TC_MODES:
             raise ValueError(f"spmm_tc {spmm_tc!r}: one of {sorted(map(str, self.TC_MODES))}")
+        if tc_kernel not in self.TC_KERNELS:
+            raise ValueError(f"tc_kernel {tc_kernel!r}: one of {sorted(self.TC_KERNELS)}")
         opts = _lib.PlanOpts(int(row_tile), int(chunk_bytes), self.TC_MODES[spmm_tc], -1 if device is None else int(device),
-                             self.SCHEDULES[schedule], self.SPLIT_LAYOUTS[split_layout])
+                             self.SCHEDULES[schedule], self.SPLIT_LAYOUTS[split_layout], self.TC_KERNELS[tc_kernel])
         h = ctypes.c_void_p()
         _lib.check(lib.sable_plan_create(ctypes.byref(desc), ctypes.byref(opts), ctypes.byref(h)), "sable_plan_create")
         del keep
@@ -56,6 +63,7 @@ class Plan:
         self.chunk_bytes = chunk_bytes
         self.schedule = schedule
         self.split_layout = split_layout
+        self.tc_kernel = tc_kernel
 
     @property
     def handle(self) -> int:
