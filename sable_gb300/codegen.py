@@ -117,7 +117,7 @@ def gen_multi_threaded_spmv(threads, val, indx, bindx, rpntr, cpntr, bpntrb, bpn
 
 
 def vbr_spmv_codegen(filename: str, dir_name: str, vbr_dir: str, threads: int, bench: int = 5, **plan_opts) -> int:
-    arrays = fileio.read_vbrc(os.path.join(vbr_dir, filename + ".vbrc"))
+    arrays = fileio.read_vbrc(fileio.source_path(vbr_dir, filename, ".vbrc"))
     t1 = time.time_ns() // 1_000_000
     if threads == 1:
         gen_single_threaded_spmv(*arrays, dir_name, filename, vbr_dir, bench, **plan_opts)
@@ -188,7 +188,7 @@ def gen_multi_threaded_spmm(threads, val, indx, bindx, rpntr, cpntr, bpntrb, bpn
 
 
 def vbr_spmm_codegen(filename: str, density: int, dir_name: str, vbr_dir: str, threads: int, **plan_opts) -> int:
-    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(os.path.join(vbr_dir, filename + ".vbr"))
+    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(fileio.source_path(vbr_dir, filename, ".vbr"))
     t1 = time.time_ns() // 1_000
     if threads == 1:
         gen_single_threaded_spmm(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density, dir_name, filename, vbr_dir,
@@ -219,7 +219,7 @@ def spmm(plan: Plan, X):
 
 # -- the reference's CUDA generators (unreachable there: read_vbr is not imported) --
 def vbr_spmv_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: int, **plan_opts) -> int:
-    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(os.path.join(vbr_dir, filename + ".vbr"))
+    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(fileio.source_path(vbr_dir, filename, ".vbr"))
     t1 = time.time_ns() // 1_000
     bt, dense = _density_mask(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density, integer_rule=True)
     comp = compress(np.asarray(val, dtype=np.float32), rpntr, cpntr, indx, bindx, bpntrb, bpntre, dense, bt=bt)
@@ -230,7 +230,7 @@ def vbr_spmv_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: i
 
 def vbr_spmm_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: int, spmm_tc="split3",
                           **plan_opts) -> int:
-    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(os.path.join(vbr_dir, filename + ".vbr"))
+    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(fileio.source_path(vbr_dir, filename, ".vbr"))
     t1 = time.time_ns() // 1_000
     bt, dense = _density_mask(val, indx, bindx, rpntr, cpntr, bpntrb, bpntre, density, integer_rule=True)
     comp = compress(np.asarray(val, dtype=np.float32), rpntr, cpntr, indx, bindx, bpntrb, bpntre, dense, bt=bt)
@@ -242,7 +242,7 @@ def vbr_spmm_cuda_codegen(filename: str, dir_name: str, vbr_dir: str, density: i
 
 # -- the reference's per-nonzero baselines (src/baseline.py) --------------------
 def _nonzeros_only(vbr_dir: str, filename: str):
-    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(os.path.join(vbr_dir, filename + ".vbr"))
+    val, indx, bindx, rpntr, cpntr, bpntrb, bpntre = fileio.read_vbr(fileio.source_path(vbr_dir, filename, ".vbr"))
     return compress(np.asarray(val, dtype=np.float32), rpntr, cpntr, indx, bindx, bpntrb, bpntre,
                     np.zeros(len(bindx), dtype=bool))
 

@@ -225,10 +225,11 @@ def choose_dense(val, rpntr, cpntr, indx, bindx, bpntrb, bpntre, density=None, m
 
 
 def convert_vbr_to_compressed(val, rpntr, cpntr, indx, bindx, bpntrb, bpntre, fname, dst_dir, density=None,
-                              model=None, N: int = 1, write: bool = True):
+                              model=None, N: int = 1, write: bool = True, binary: bool = False):
     """utils/convert_real_to_vbr.py:18-96; returns (val2, indx2, bindx,
     bpntrb, bpntre, ublocks, indptr, indices, csr_val) and writes
-    <dst_dir>/<fname>.vbrc (unless write=False)."""
+    <dst_dir>/<fname>.vbrc (unless write=False; binary=True writes the
+    binary form <fname>.vbrcb instead)."""
     val = np.asarray(val, dtype=np.float64)
     bt = block_table(rpntr, cpntr, bpntrb, bpntre, bindx, indx)
     dense = choose_dense(val, rpntr, cpntr, indx, bindx, bpntrb, bpntre, density=density, model=model, N=N, bt=bt)
@@ -237,8 +238,9 @@ def convert_vbr_to_compressed(val, rpntr, cpntr, indx, bindx, bpntrb, bpntre, fn
     indices = c.indices if c.indices is not None else np.zeros(0, dtype=np.int64)
     csr_val = c.csr_val if c.csr_val is not None else np.zeros(0)
     if write:
-        fileio.write_vbrc(os.path.join(dst_dir, f"{fname}.vbrc"), c.val, csr_val, indptr, indices, c.indx,
-                          bindx, rpntr, cpntr, bpntrb, bpntre, c.ublocks)
+        writer = fileio.write_vbrc_binary if binary else fileio.write_vbrc
+        writer(os.path.join(dst_dir, f"{fname}.vbrc" + ("b" if binary else "")), c.val, csr_val, indptr, indices,
+               c.indx, bindx, rpntr, cpntr, bpntrb, bpntre, c.ublocks)
     return c.val, c.indx, np.asarray(bindx), np.asarray(bpntrb), np.asarray(bpntre), c.ublocks, indptr, indices, csr_val
 
 

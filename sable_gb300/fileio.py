@@ -14,8 +14,10 @@ Dense operands: ``Generated_dense_tensors/generated_vector_{n}.vector`` and
 Values are written with Python's ``str`` of each element, as the reference
 does, so the files are byte-identical for identical inputs.  Readers return
 numpy arrays (float64 values, int64 indices) instead of lists; parsing is
-vectorised.  ``.vbrb`` is a binary (npz) form of either file for large
-matrices, where text parsing dominates end-to-end time.
+vectorised.  ``.vbrb`` and ``.vbrcb`` are binary (npz) forms of ``.vbr`` and
+``.vbrc`` for large matrices, where text parsing dominates end-to-end time;
+read_vbr / read_vbrc accept them, and the *_codegen entry points read the
+binary form when the text file is absent (source_path).
 """
 from __future__ import annotations
 
@@ -112,9 +114,40 @@ def read_dense_values(path: str) -> np.ndarray:
     return np.array(text.split(","), dtype=np.float64)
 
 
+def source_path(dir_name: str, filename: str, ext: str) -> str:
+    """Path of matrix `filename` in `dir_name` with text suffix `ext` (".vbr"
+    or ".vbrc"): the text file when it exists, else its binary form (".vbrb" /
+    ".vbrcb") when that exists, else the text path (so that a missing matrix
+    is reported under the reference's file name)."""
+    text = join(dir_name, filename + ext)
+    if exists(text):
+        return text
+    binary = text + "b"
+    return binary if exists(binary) else text
+
+
+def write_vbr_binary(filename: str, vbr_matrix: VBR, dir_name: str) -> str:
+    """Binary counterpart of write_vbr_matrix: <dir_name>/<filename>.vbrb."""
+    os.makedirs(dir_name, exist_ok=True)
+    path = join(dir_name, filename + ".vbrb")
+    write_binary(path, **dict(zip(VBR_FIELDS, vbr_matrix.arrays())))
+    return path
+
+
+def write_vbrc_binary(path: str, val2, csr_val, indptr, indices, indx2, bindx, rpntr, cpntr, bpntrb, bpntre,
+                      ublocks) -> None:
+    """Binary counterpart of write_vbrc (argument order of the .vbrc lines);
+    `path` ends in .vbrcb."""
+    write_binary(path, **dict(zip(VBRC_FIELDS, (val2, csr_val, indptr, indices, indx2, bindx, rpntr, cpntr, bpntrb,
+                                                bpntre, ublocks))))
+
+
 def read_vbr(filename: str):
     """utils/fileio.py:55-64 -> (val, indx, bindx, rpntr, cpntr, bpntrb, bpntre)."""
-    if filename.endswith(".vbrb"):
+    if filename.endswith(".vbrb") or filename.endswith(".vbrcb"):
+        with np.load(filename) as z:
+            if "ublocks" in z:
+                raise ValueError(f"{filename}: holds a compressed (.vbrc) matrix; read it with read_vbrc")
         return read_binary(filename, VBR_FIELDS)
     with open(filename) as f:
         val = _parse_line(f.readline(), np.float64)
@@ -125,7 +158,10 @@ def read_vbr(filename: str):
 def read_vbrc(filename: str):
     """utils/fileio.py:66-93 -> (val, indx, bindx, rpntr, cpntr, bpntrb,
     bpntre, ublocks, indptr, indices, csr_val)."""
-    if filename.endswith(".vbrb"):
+    if filename.endswith(".vbrcb") or filename.endswith(".vbrb"):
+        with np.load(filename) as z:
+            if "ublocks" not in z:
+                raise ValueError(f"{filename}: holds an uncompressed (.vbr) matrix; read it with read_vbr")
         d = read_binary(filename, VBRC_FIELDS)
         got = dict(zip(VBRC_FIELDS, d))
     else:
