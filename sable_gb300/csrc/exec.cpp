@@ -199,6 +199,7 @@ static int build_umma_planes(sable_plan *p, const Layout &L, int64_t *bytes) {
         memcpy(&hd, L.records.data() + table[idx].off, sizeof hd);
         if (hd.nq <= 0) continue;
         const int64_t hp = (hd.h + 15) & ~15, nks = (4 * (int64_t)hd.nq + 15) / 16;
+        p->umma_hp = std::max<int>(p->umma_hp, (int)hp);
         off[idx] = total;
         total += nks * TERMS * hp * 32;
     }
@@ -348,6 +349,7 @@ int launch_spmm_plan(const sable_plan *p, LaunchArgs &a, int N, int nt, bool tim
     a.tcoff = p->d_tcoff;
     a.umma = p->d_umma;
     a.umma_off = p->d_umma_off;
+    a.umma_hp = p->umma_hp;
     const int64_t part_stride = p->n_partial * nt;
     if (p->spmm_tc && N >= 32) {
         const int terms = p->spmm_tc == SABLE_TC_SPLIT3 ? 3 : 2;

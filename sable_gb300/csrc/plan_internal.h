@@ -60,6 +60,7 @@ struct sable_plan {
     int64_t *d_umma_off = nullptr;       // byte offset of each item's terms (item-table order), -1: none
     std::vector<int64_t> umma_off_host;  // the same on the host
     int64_t umma_bytes = 0;
+    int umma_hp = 16;                    // tallest tile with a panel, rounded up to 16
     float *d_ppartial = nullptr;         // multi-part tile partials
     int *d_pcounters = nullptr;          // multi-part tile counters
     int64_t n_parts = 0, n_multi = 0;

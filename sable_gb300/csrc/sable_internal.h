@@ -164,6 +164,7 @@ struct LaunchArgs {
     const int64_t *tcoff;   // word offset of each item's fragments in tcplanes (item-table order)
     const unsigned char *umma;    // SpMM split-BF16 on tcgen05: panel terms in the UMMA K-major layout
     const int64_t *umma_off;      // byte offset of each item's terms in umma (item-table order), -1: none
+    int umma_hp;                  // tallest tile with a panel, rounded up to 16 (sizes the panel ring)
     int *error;             // set to 1 when a bounded device wait runs out
     int n_items;
     int stage_bytes;        // TMA staging bytes per stage (>= largest record)

@@ -351,6 +351,7 @@ __device__ __forceinline__ void spmm_tile_finish(const unsigned char *R, const I
     __shared__ int s_last;
     __shared__ int s_wrow[9];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool act = tid < SABLE_THREADS;   // CTAs of more threads: the others only meet the barriers
     const int cq = lane % CQ, rs = lane / CQ;
     const int h = c.h, n0 = slice * NT;
     const float *__restrict__ X = a.x;
@@ -360,7 +361,8 @@ __device__ __forceinline__ void spmm_tile_finish(const unsigned char *R, const I
     if (c.ns > 0) {
         const uint2 *__restrict__ E = reinterpret_cast<const uint2 *>(R + c.csr_off);
         const int ns = c.ns;
-        for (int i = tid; i <= h; i += SABLE_THREADS) rst[i] = __ldg(reinterpret_cast<const int *>(R + c.rp_off) + i);
+        if (act)
+            for (int i = tid; i <= h; i += SABLE_THREADS) rst[i] = __ldg(reinterpret_cast<const int *>(R + c.rp_off) + i);
         __syncthreads();
         if (warp == 0 && lane < 9) {
             const int target = (int)(((int64_t)ns * lane) / 8);
@@ -372,7 +374,7 @@ __device__ __forceinline__ void spmm_tile_finish(const unsigned char *R, const I
             s_wrow[lane] = lane == 8 ? h : lo;
         }
         __syncthreads();
-        for (int r = s_wrow[warp]; r < s_wrow[warp + 1]; ++r) {
+        for (int r = act ? s_wrow[warp] : 0; r < (act ? s_wrow[warp + 1] : 0); ++r) {
             const int b = rst[r], e = rst[r + 1];
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
             for (int base = b; base < e; base += RSUB) {
@@ -398,7 +400,7 @@ __device__ __forceinline__ void spmm_tile_finish(const unsigned char *R, const I
     // ---- output -------------------------------------------------------------------
     const bool split = c.nitem > 1;
     const int64_t pbase = (int64_t)slice * part_stride + (c.part_base + (int64_t)c.kidx * h) * NT;
-    for (int e = tid; e < h * CQ; e += SABLE_THREADS) {
+    for (int e = tid; act && e < h * CQ; e += SABLE_THREADS) {
         const int i = e / CQ, q = e - i * CQ, n = n0 + 4 * q;
         if (n >= a.N) continue;
         const float4 v = ys4[i * CQ + q];
@@ -414,7 +416,7 @@ __device__ __forceinline__ void spmm_tile_finish(const unsigned char *R, const I
         __syncthreads();
         if (s_last) {
             const int64_t tb = (int64_t)slice * part_stride + c.part_base * NT;
-            for (int e = tid; e < h * CQ; e += SABLE_THREADS) {
+            for (int e = tid; act && e < h * CQ; e += SABLE_THREADS) {
                 const int i = e / CQ, q = e - i * CQ, n = n0 + 4 * q;
                 if (n >= a.N) continue;
                 float4 s = make_float4(0.f, 0.f, 0.f, 0.f);

@@ -1,5 +1,8 @@
 // Split-BF16 SpMM of one (item record, N-slice) unit on the tcgen05 tensor
-// cores, by one CTA of SABLE_THREADS threads.  Replaces the dense-block part
+// cores, by one CTA of UMMA_THREADS threads: SABLE_THREADS producer threads
+// (warps 0-7) and one issuer warp (warp 8) whose lane 0 alone starts the bulk
+// copies and issues the MMAs, so that the producers never wait on that
+// serial work.  Replaces the dense-block part
 // of gen_single_threaded_spmm (src/codegen.py:827-937; spmm_kernel, :851-859)
 // for plans built with spmm_tc and N >= 32; the CSR entries of the item stay
 // FP32 on the CUDA cores (spmm_tile_finish).
@@ -18,12 +21,15 @@
 //              is built, in the UMMA K-major layout (umma.cuh): per step 3
 //              blocks of hp x 32 bytes (hp = h rounded up to 16); one bulk
 //              copy (cp.async.bulk, mbarrier completion) brings TERMS of them
-//              into a ring of BST stages, BST - 2 steps ahead of the MMAs.
+//              into a ring of bst stages, bst - 2 steps ahead of the MMAs
+//              (bst = 4..8, as many stages of the plan's tallest tile as fit
+//              beside three CTAs per SM; LaunchArgs.umma_bst / umma_bstage).
 //   A operand  the 16 X rows of the step (NT floats each, from L2), loaded
-//              one step ahead into registers with 16-byte loads, split into
-//              TERMS BF16 terms by the CTA and stored in the MN-major layout
-//              (8-byte stores, conflict-free) into a ring of 2 stages.
-//   MMA        thread 0 waits for the step's panel copy, issues the TERMS
+//              two steps ahead into registers with 16-byte loads (their row
+//              indices four steps ahead, so no load waits on another), split
+//              into TERMS BF16 terms by the CTA and stored in the MN-major
+//              layout (8-byte stores, conflict-free) into a ring of 2 stages.
+//   MMA        the issuer waits for the step's panel copy, issues the TERMS
 //              products (tcgen05.mma.cta_group::1.kind::f16, M = 128, N = hp,
 //              K = 16) and commits them to the step parity's mbarrier; the
 //              CTA waits for the products of step ks - 2 before it reuses
@@ -38,21 +44,26 @@
 
 namespace {
 
-constexpr int UMMA_BST = 4;                 // panel-term stages (bulk-copy ring)
-constexpr int UMMA_LOOK = UMMA_BST - 2;     // panel copies issued this many steps ahead
+constexpr int UMMA_BST_MIN = 4, UMMA_BST_MAX = 8;   // panel-term stages (bulk-copy ring)
 constexpr int UMMA_M = 128;                 // MMA rows (TMEM lanes)
-constexpr int UMMA_STEP_BLOCK = SABLE_MAX_ROW_TILE * 32;  // bytes of one term block of a step (hp <= 128)
+constexpr int UMMA_THREADS = SABLE_THREADS + 32;   // producers + the issuer warp
+// Dynamic shared memory of one CTA when three CTAs share an SM (228 KB less
+// the per-CTA reserve and static shared memory).
+constexpr int UMMA_SMEM_BUDGET = 75776;
 
+// Shared memory of a CTA: 2 stages of X terms, bst stages of panel terms of
+// bstage bytes, then the CSR row starts; the Y tile reuses the stage space.
 template <int NT, int TERMS>
 struct UmmaSmem {
     static constexpr int A_STAGE = TERMS * UMMA_M * 32;       // X terms of one step (MN-major, 128 rows)
-    static constexpr int B_STAGE = TERMS * UMMA_STEP_BLOCK;   // panel terms of one step
     static constexpr int OFF_A = 0;                           // 2 stages
-    static constexpr int OFF_B = OFF_A + 2 * A_STAGE;         // UMMA_BST stages
-    static constexpr int LOOP = OFF_B + UMMA_BST * B_STAGE;
+    static constexpr int OFF_B = OFF_A + 2 * A_STAGE;         // bst stages
     static constexpr int YS = SABLE_MAX_ROW_TILE * NT * 4;    // Y tile (after the K loop, over the stages)
-    static constexpr int OFF_RST = (YS > LOOP ? YS : LOOP);
-    static constexpr int TOTAL = OFF_RST + (SABLE_MAX_ROW_TILE + 8) * 4;
+    static constexpr int RST = (SABLE_MAX_ROW_TILE + 8) * 4;
+    __host__ __device__ static constexpr int off_rst(int bst, int bstage) {
+        return YS > OFF_B + bst * bstage ? YS : OFF_B + bst * bstage;
+    }
+    __host__ __device__ static constexpr int total(int bst, int bstage) { return off_rst(bst, bstage) + RST; }
 };
 
 // Split four FP32 values into TERMS BF16 terms; t[k] packs the four k-th
@@ -72,23 +83,40 @@ __device__ __forceinline__ void split4(const float4 v, uint2 (&t)[TERMS]) {
     }
 }
 
+// Read-only global loads whose issue point the compiler keeps (asm volatile):
+// the K loop loads X two steps and its row indices four steps before use,
+// and a load moved down to its use would wait out the memory latency.
+__device__ __forceinline__ float4 ld_pinned_f4(const float *p) {
+    float4 v;
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+__device__ __forceinline__ int ld_pinned_s32(const int *p) {
+    int v;
+    asm volatile("ld.global.nc.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
 // Unit u of a step's X gather (4 NT units of one float4): lane bits pick
 // (k & 7) and the low bits of the M quad so that a warp's 8-byte term stores
-// cover 256 contiguous bytes of the MN-major block (no bank conflicts).
+// cover 256 contiguous bytes of the MN-major block (no bank conflicts).  The
+// units of one thread (u = tid + 256 i) share k.
 __device__ __forceinline__ void umma_unit(int u, int &k, int &q) {
     k = ((u >> 1) & 7) | (((u >> 5) & 1) << 3);
     q = (u & 1) | (((u >> 4) & 1) << 1) | ((u >> 6) << 2);
 }
 
-// planes: the item's panel terms (3 term blocks of hp x 32 bytes per step).
+// planes: the item's panel terms (3 term blocks of hp x 32 bytes per step);
+// bst / bstage: the panel ring (stages, bytes per stage >= TERMS hp 32).
 template <int NT, int TERMS>
 __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const MatIO &a, int slice, int64_t part_stride,
-                                               unsigned char *smem, const unsigned char *planes, int *error) {
+                                               unsigned char *smem, const unsigned char *planes, int *error, int bst,
+                                               int bstage) {
     using L = UmmaSmem<NT, TERMS>;
     constexpr int UNITS = 4 * NT;                                    // float4 loads per step
     constexpr int UPT = (UNITS + SABLE_THREADS - 1) / SABLE_THREADS; // per thread
     constexpr int NPROD = TERMS == 3 ? 6 : 3;
-    __shared__ __align__(8) uint64_t s_full[UMMA_BST];   // panel copy of a stage landed
+    __shared__ __align__(8) uint64_t s_full[UMMA_BST_MAX];   // panel copy of a stage landed
     __shared__ __align__(8) uint64_t s_done[2];          // products of steps of that parity completed
     __shared__ uint32_t s_taddr;
     // abort flags: [ks & 1] is written before and read after the barrier of
@@ -97,12 +125,15 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
     __shared__ int s_abort[3];
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool prod = tid < SABLE_THREADS;          // producer threads
+    const bool issuer = tid == SABLE_THREADS;       // lane 0 of warp 8
     const ItemHeader c = *reinterpret_cast<const ItemHeader *>(R);
     const int h = c.h, nq = c.nq, ncol = 4 * nq;
     const int n0 = slice * NT;
     float *ys = reinterpret_cast<float *>(smem);
     float4 *ys4 = reinterpret_cast<float4 *>(smem);
-    int *rst = reinterpret_cast<int *>(smem + L::OFF_RST);
+    int *rst = reinterpret_cast<int *>(smem + L::off_rst(bst, bstage));
+    const int look = bst - 2;    // panel copies run this many steps ahead
 
     if (nq > 0) {
         const int nks = (ncol + 15) >> 4;
@@ -115,7 +146,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         const int *colmap = reinterpret_cast<const int *>(R + c.xcol_off);
         const float *__restrict__ X = a.x;
         if (tid == 0) {
-            for (int s = 0; s < UMMA_BST; ++s) mbar_init(smem_addr(&s_full[s]));
+            for (int s = 0; s < bst; ++s) mbar_init(smem_addr(&s_full[s]));
             mbar_init(smem_addr(&s_done[0]));
             mbar_init(smem_addr(&s_done[1]));
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -126,51 +157,60 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         __syncthreads();
         tc_fence_after();
         const uint32_t taddr = s_taddr;
-        // panel copies of the first UMMA_LOOK steps
-        if (tid == 0)
-            for (int j = 0; j < UMMA_LOOK && j < nks; ++j)
-                tma_record(smem_addr(&s_full[j]), smem + L::OFF_B + j * L::B_STAGE, planes + (size_t)j * step_src,
+        // panel copies of the first `look` steps
+        if (issuer)
+            for (int j = 0; j < look && j < nks; ++j)
+                tma_record(smem_addr(&s_full[j]), smem + L::OFF_B + j * bstage, planes + (size_t)j * step_src,
                            copy_bytes);
-        // X rows of step 0 into registers
-        float4 xr[UPT];
-        auto load_step = [&](int ks) {
+        // this thread's panel column within a step, and its X row at step j (-1: none)
+        int k0, q0;
+        umma_unit(tid, k0, q0);
+        auto col_row = [&](int j) -> int {
+            const int col = 16 * j + k0;
+            return (prod && tid < UNITS && j < nks && col < ncol) ? ld_pinned_s32(colmap + col) : -1;
+        };
+        auto load_step = [&](int row, float4 (&dst)[UPT]) {
 #pragma unroll
             for (int i = 0; i < UPT; ++i) {
                 const int u = tid + i * SABLE_THREADS;
                 int k, q;
                 umma_unit(u, k, q);
-                const int col = 16 * ks + k, n = n0 + 4 * q;
-                xr[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (u < UNITS && col < ncol && n < a.N)
-                    xr[i] = __ldg(reinterpret_cast<const float4 *>(X + (int64_t)__ldg(colmap + col) * a.ldx + n));
+                const int n = n0 + 4 * q;
+                dst[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (prod && u < UNITS && row >= 0 && n < a.N)
+                    dst[i] = ld_pinned_f4(X + (int64_t)row * a.ldx + n);
             }
         };
-        load_step(0);
-        bool bad = false;       // thread 0: a panel copy wait ran out (published before the next barrier)
-        int issued = UMMA_LOOK < nks ? UMMA_LOOK : nks, landed = 0;   // thread 0: panel copies
+        bool bad = false;       // issuer: a panel copy wait ran out (published before the next barrier)
+        int issued = look < nks ? look : nks, landed = 0;   // issuer: panel copies
         int steps_run = nks;    // steps whose products were committed (uniform across the CTA)
-        for (int ks = 0; ks < nks; ++ks) {
+        // Step ks: its X values are in `slot` (loaded two steps earlier), which
+        // then receives those of step ks + 2, whose row `cm` was read two steps
+        // earlier still; `cm` then receives the row of step ks + 4.  false:
+        // the CTA stops (abort; uniform).
+        auto step = [&](int ks, float4 (&slot)[UPT], int &cm) -> bool {
             // the products of step ks - 2 have read their A stage (ks & 1) and
-            // their panel stage ((ks + UMMA_LOOK) % UMMA_BST)
+            // their panel stage ((ks + look) % bst)
             if (ks >= 2 && !mbar_wait(smem_addr(&s_done[ks & 1]), (uint32_t)(((ks - 2) >> 1) & 1))) s_abort[ks & 1] = 1;
-            if (tid == 0) {
+            if (issuer) {
                 if (bad) s_abort[ks & 1] = 1;
-                const int j = ks + UMMA_LOOK;
+                const int j = ks + look;
                 if (j < nks) {
-                    tma_record(smem_addr(&s_full[j % UMMA_BST]), smem + L::OFF_B + (j % UMMA_BST) * L::B_STAGE,
+                    tma_record(smem_addr(&s_full[j % bst]), smem + L::OFF_B + (j % bst) * bstage,
                                planes + (size_t)j * step_src, copy_bytes);
                     issued = j + 1;
                 }
             }
             float4 cur[UPT];
 #pragma unroll
-            for (int i = 0; i < UPT; ++i) cur[i] = xr[i];
-            if (ks + 1 < nks) load_step(ks + 1);
+            for (int i = 0; i < UPT; ++i) cur[i] = slot[i];
+            load_step(cm, slot);
+            cm = col_row(ks + 4);
             unsigned char *As = smem + L::OFF_A + (ks & 1) * L::A_STAGE;
 #pragma unroll
             for (int i = 0; i < UPT; ++i) {
                 const int u = tid + i * SABLE_THREADS;
-                if (u < UNITS) {
+                if (prod && u < UNITS) {
                     int k, q;
                     umma_unit(u, k, q);
                     uint2 t[TERMS];
@@ -184,15 +224,15 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
             __syncthreads();
             if (s_abort[ks & 1]) {
                 steps_run = ks;
-                break;
+                return false;
             }
-            if (tid == 0) {
-                const int s = ks % UMMA_BST;
-                if (mbar_wait(smem_addr(&s_full[s]), (uint32_t)((ks / UMMA_BST) & 1))) {
+            if (issuer) {
+                const int s = ks % bst;
+                if (mbar_wait(smem_addr(&s_full[s]), (uint32_t)((ks / bst) & 1))) {
                     landed = ks + 1;
                     tc_fence_after();
                     const uint32_t a_st = a_base + (uint32_t)((ks & 1) * L::A_STAGE);
-                    const uint32_t b_st = b_base + (uint32_t)(s * L::B_STAGE);
+                    const uint32_t b_st = b_base + (uint32_t)(s * bstage);
                     // products (x term, panel term), smallest first
                     constexpr int PA[6] = {1, 0, 2, 0, 1, 0}, PB[6] = {1, 2, 0, 1, 0, 0};
                     constexpr int QA[3] = {0, 1, 0}, QB[3] = {1, 0, 0};
@@ -208,16 +248,25 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 }
                 umma_commit(smem_addr(&s_done[ks & 1]));
             }
+            return true;
+        };
+        float4 xr0[UPT], xr1[UPT];   // X values of the next even / odd step
+        load_step(col_row(0), xr0);
+        load_step(col_row(1), xr1);
+        int cm0 = col_row(2), cm1 = col_row(3);
+        for (int ks = 0; ks < nks; ks += 2) {
+            if (!step(ks, xr0, cm0)) break;
+            if (ks + 1 < nks && !step(ks + 1, xr1, cm1)) break;
         }
         // Every product issued has completed before TMEM is read or freed:
         // a commit tracks the MMAs issued since the previous commit, and the
         // MMAs of one accumulator complete in issue order, so the last step's
         // commit covers them all.  Every panel copy issued has landed before
         // the CTA exits.
-        if (tid == 0) {
+        if (issuer) {
             if (bad) s_abort[2] = 1;
             for (int j = landed; j < issued; ++j)
-                if (!mbar_wait(smem_addr(&s_full[j % UMMA_BST]), (uint32_t)((j / UMMA_BST) & 1))) s_abort[2] = 1;
+                if (!mbar_wait(smem_addr(&s_full[j % bst]), (uint32_t)((j / bst) & 1))) s_abort[2] = 1;
         }
         if (steps_run > 0) {
             const int last = steps_run - 1;
@@ -232,7 +281,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
             // lane m of quadrant (warp & 3) -> Y column n0 + m; the two warp
             // halves take alternate 16-column chunks of the accumulator
             const int quad = warp & 3, m = 32 * quad + lane;
-            if (32 * quad < NT) {
+            if (prod && 32 * quad < NT) {
                 for (int c0 = 16 * (warp >> 2); c0 < hp; c0 += 32) {
                     uint32_t r[16];
                     tmem_ld16(taddr + ((uint32_t)(32 * quad) << 16) + (uint32_t)c0, r);
@@ -249,7 +298,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
             tmem_free(taddr, ncols);
         }
     } else {
-        for (int e = tid; e < h * (NT / 4); e += SABLE_THREADS) ys4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int e = tid; e < h * (NT / 4); e += UMMA_THREADS) ys4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     spmm_tile_finish<NT>(R, c, a, slice, part_stride, ys4, rst);
 }
