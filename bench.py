@@ -247,7 +247,9 @@ def bench_batch(reps: int) -> dict:
     for m, w in zip(mats, widths):
         xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
         ys.append(torch.empty(m.n_rows if w == 1 else (m.n_rows, w), device="cuda"))
-    plain, learned = [], []
+    from oracle import oracle
+    plain, learned, learned_comps = [], [], []
+    errs_med = []
     nnz_work = 0
     for m, w in zip(mats, widths):
         bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
@@ -256,8 +258,9 @@ def bench_batch(reps: int) -> dict:
         lay = "mixed" if w == 1 else "separate"
         plain.append(Plan(convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, rf, bt=bt),
                           split_layout=lay))
-        learned.append(Plan(convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mlp,
-                                             bt=bt), spmm_tc="split3", split_layout=lay))
+        learned_comps.append(convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mlp,
+                                              bt=bt))
+        learned.append(Plan(learned_comps[-1], spmm_tc="split3", split_layout=lay))
 
     def run_plain():
         for p, x, y, w in zip(plain, xs, ys, widths):
@@ -270,6 +273,16 @@ def bench_batch(reps: int) -> dict:
     batch, table = autotune.tune_batch(learned, widths, xs, ys)
     ms_b = autotune.time_ms(lambda: batch.run(xs, ys), reps)
     info = batch.info()
+    # every one of the batch's outputs against the FP64 oracle
+    batch.run(xs, ys)
+    batch.check()
+    errs = []
+    for m, w, x, y, p in zip(mats, widths, xs, ys, learned_comps):
+        xn = x.cpu().numpy()
+        yr, ya = oracle.spmv_vbrc(p, xn) if w == 1 else oracle.spmm_vbr(m, xn)
+        r = oracle.report(y.cpu().numpy(), yr, ya)
+        errs.append(r["max"])
+        errs_med.append(r["median"])
     for p in plain + learned:
         p.close()
     batch.close()
@@ -278,6 +291,9 @@ def bench_batch(reps: int) -> dict:
             "plain_ms": round(ms_p, 4), "plain_launches": len(mats) + sum(1 for w in widths if w == 1),
             "learned_batched_ms": round(ms_b, 4), "learned_vs_plain": round(ms_p / ms_b, 3),
             "work_gflop": round(2 * nnz_work / 1e9, 3), "learned_batched_gflops": round(2 * nnz_work / (ms_b * 1e6), 1),
+            "error_vs_fp64_scaled": {"max": float(np.max(errs)), "median": float(np.median(errs_med)),
+                                     "matrices": len(errs), "tolerance": oracle.TOL,
+                                     "measure": "per output |y - y_fp64| / (|A||x|), all 256 matrices"},
             "batch": {"n_units": info["n_units"], "n_ctas": info["n_ctas"], "stages": info["stages"],
                       "graph": True, "tuning": table}}
 

@@ -240,6 +240,51 @@ int sable_batch_check(sable_batch *batch, void *stream);
 int sable_batch_get_info(const sable_batch *batch, sable_batch_info *out);
 int sable_batch_destroy(sable_batch *batch);
 
+/*
+ * GPU inspector steps upstream of the plan (no plan needed).  Inputs are host
+ * arrays; the functions upload them, run on the device (current device when
+ * `device` < 0) and synchronise.
+ */
+typedef struct sable_csr_desc {
+    int32_t n_rows, n_cols;
+    const int64_t *indptr;   /* n_rows + 1 entries, from 0 to nnz, non-decreasing */
+    const int32_t *indices;  /* column of every entry, 0 <= c < n_cols          */
+    const void *data;        /* value of every entry: FP32 or FP64               */
+    int32_t value_bytes;     /* 4 or 8                                           */
+    int64_t nnz;
+} sable_csr_desc;
+
+/* VBR construction from a CSR matrix and its partition: replaces
+ * convert_sparse_to_vbr (utils/convert_real_to_vbr.py:98-199).  Every
+ * (rpntr x cpntr) block holding at least one stored entry (explicit zeros
+ * count) becomes a stored block, dense and column-major, in block-row order,
+ * ascending block column; duplicate entries are summed in CSR order.  Values
+ * keep the CSR's type.  A block row without a stored entry gets
+ * bpntrb = bpntre = -1 (the reference asserts that none exists).
+ * SABLE_ERR_UNSUPPORTED when a block row's bitmap of n_block_cols bits does
+ * not fit in shared memory (about 1.5 million block columns). */
+typedef struct sable_vbr_build sable_vbr_build;
+int sable_vbr_from_csr(const sable_csr_desc *csr, int32_t n_block_rows, const int32_t *rpntr, int32_t n_block_cols,
+                       const int32_t *cpntr, int32_t device, sable_vbr_build **out);
+/* Number of stored blocks and of values (val holds n_val entries of the
+ * CSR's value type; indx n_blocks + 1; bpntrb / bpntre n_block_rows). */
+int sable_vbr_build_sizes(const sable_vbr_build *build, int64_t *n_blocks, int64_t *n_val);
+int sable_vbr_build_copy(const sable_vbr_build *build, void *val, int64_t *indx, int32_t *bindx, int32_t *bpntrb,
+                         int32_t *bpntre);
+int sable_vbr_build_destroy(sable_vbr_build *build);
+
+/* Row and column partition by adjacent-line similarity: replaces cut_indices2
+ * (src/autopartition.py:34-68) with similarity2 (:87-89, mode 0) or its numba
+ * variant similarity2_numba (:91-107, mode 1, which scores a pair with an
+ * all-zero line 0 instead of NaN).  `csr` is the matrix, `csc` its transpose
+ * in CSR form (the matrix's CSC); indices must increase strictly within each
+ * line.  Writes the row cuts (rpntr, at most n_rows + 1 entries) and the
+ * column cuts (cpntr, at most n_cols + 1), each starting at 0 and ending at
+ * the dimension, and their counts.  Similarities are computed in FP64. */
+int sable_similarity_cuts(const sable_csr_desc *csr, const sable_csr_desc *csc, double threshold, int32_t mode,
+                          int32_t device, int32_t *rpntr_out, int32_t *n_rpntr, int32_t *cpntr_out,
+                          int32_t *n_cpntr);
+
 /* Block features for the block model, one row of 6 floats per stored block
  * (bindx order): rows, cols, nnz, density, variance of nnz per row, N.
  * Host-side; `desc` must be uncompressed (all blocks in val). */

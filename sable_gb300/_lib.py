@@ -7,7 +7,7 @@ from __future__ import annotations
 
 import ctypes
 import threading
-from ctypes import POINTER, c_char_p, c_float, c_int, c_int32, c_int64, c_void_p
+from ctypes import c_double, POINTER, c_char_p, c_float, c_int, c_int32, c_int64, c_void_p
 
 import numpy as np
 
@@ -43,6 +43,11 @@ class VbrcDesc(ctypes.Structure):
 class PlanOpts(ctypes.Structure):
     _fields_ = [("row_tile", c_int32), ("chunk_bytes", c_int32), ("spmm_tc", c_int32), ("device", c_int32),
                 ("schedule", c_int32), ("split_layout", c_int32), ("tc_kernel", c_int32)]
+
+
+class CsrDesc(ctypes.Structure):
+    _fields_ = [("n_rows", c_int32), ("n_cols", c_int32), ("indptr", c_void_p), ("indices", c_void_p),
+                ("data", c_void_p), ("value_bytes", c_int32), ("nnz", c_int64)]
 
 
 class PlanStats(ctypes.Structure):
@@ -84,6 +89,13 @@ SIGNATURES = {
     "sable_batch_get_info": (c_int, [c_void_p, POINTER(BatchInfo)]),
     "sable_batch_destroy": (c_int, [c_void_p]),
     "sable_block_features": (c_int, [POINTER(VbrcDesc), c_int32, c_void_p]),
+    "sable_vbr_from_csr": (c_int, [POINTER(CsrDesc), c_int32, c_void_p, c_int32, c_void_p, c_int32,
+                                   POINTER(c_void_p)]),
+    "sable_vbr_build_sizes": (c_int, [c_void_p, POINTER(c_int64), POINTER(c_int64)]),
+    "sable_vbr_build_copy": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sable_vbr_build_destroy": (c_int, [c_void_p]),
+    "sable_similarity_cuts": (c_int, [POINTER(CsrDesc), POINTER(CsrDesc), c_double, c_int32, c_int32, c_void_p,
+                                      POINTER(c_int32), c_void_p, POINTER(c_int32)]),
     "sable_mlp_create": (c_int, [POINTER(c_void_p)]),
     "sable_mlp_destroy": (c_int, [c_void_p]),
     "sable_mlp_set_params": (c_int, [c_void_p, c_void_p]),

@@ -340,3 +340,51 @@ def vbr_matrix_gen(m: int, n: int, partitioning: str, row_split: int, col_split:
         name = f"Matrix_{m}_{n}_{row_split}_{col_split}_{num_dense}_{perc_dense_zeros}_{num_sparse}_{partitioning}"
         write_vbr_matrix(name, matrix, vbr_dir + "_Sparse")
     return name
+
+
+def partition_case(seed: int, n_rows: int, n_cols: int, values: str = "quarters", empty_lines: bool = True,
+                   explicit_zeros: bool = True):
+    """A sparse matrix with hidden block structure for the partitioning steps
+    (similarity cuts, VBR construction): blocks of 1..24 rows / columns, 15 %
+    of them present with density U[0.3, 1], a few scattered entries, runs of
+    empty rows and columns (first and last lines included) and stored zeros.
+    values "quarters": multiples of 1/4 in [-2.25, 2.25] (every product and sum
+    exact in FP64, so any summation order agrees); "uniform": U(-1, 1).
+    Returns a canonical scipy CSR array (explicit zeros kept)."""
+    import scipy.sparse
+    rng = np.random.default_rng(seed)
+    rs = sizes_until(rng, 1, 24, n_rows)
+    cs = sizes_until(rng, 1, 24, n_cols)
+    rp = np.concatenate([[0], np.cumsum(rs)])
+    cp = np.concatenate([[0], np.cumsum(cs)])
+    mask = np.zeros((n_rows, n_cols), dtype=bool)
+    for i in range(len(rs)):
+        for j in range(len(cs)):
+            if rng.random() < 0.15:
+                d = rng.uniform(0.3, 1.0)
+                mask[rp[i]:rp[i + 1], cp[j]:cp[j + 1]] = rng.random((rs[i], cs[j])) < d
+    mask |= rng.random((n_rows, n_cols)) < 0.002
+    if empty_lines:
+        for k in rng.choice(n_rows, size=max(1, n_rows // 40), replace=False):
+            mask[k: k + int(rng.integers(1, 4)), :] = False
+        for k in rng.choice(n_cols, size=max(1, n_cols // 40), replace=False):
+            mask[:, k: k + int(rng.integers(1, 4))] = False
+        mask[0, :] = False
+        mask[:, -1] = False
+    r, c = np.nonzero(mask)
+    if values == "quarters":
+        v = rng.integers(-9, 10, size=len(r)).astype(np.float64) / 4.0
+        v[v == 0] = 0.25
+    else:
+        v = rng.uniform(-1.0, 1.0, size=len(r))
+    if explicit_zeros and len(v):
+        v[rng.random(len(v)) < 0.02] = 0.0
+    A = scipy.sparse.csr_array((v, (r, c)), shape=(n_rows, n_cols))
+    A.sum_duplicates()
+    return A
+
+
+# (seed, n_rows, n_cols, values, empty_lines) of the partition fixtures
+PARTITION_CASES = [(3001, 300, 260, "quarters", True), (3002, 500, 420, "quarters", False),
+                   (3003, 240, 300, "uniform", False), (3004, 160, 150, "quarters", True),
+                   (3005, 700, 640, "quarters", False)]

@@ -1,11 +1,13 @@
 """Generate the golden fixtures of tests/golden/ from the reference itself.
 
-Run in a container that holds the reference at /root/reference (read-only):
+Run in a container that holds the reference tree (read-only), naming its root
+as the argument or in SABLE_REFERENCE_ROOT:
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py <reference root>
 
-Steps (harness shims only, all inside a scratch copy under /tmp):
-  1. copy the reference tree to /tmp/sable_ref_golden;
+Steps (harness shims only, all inside a scratch copy in a temporary
+directory):
+  1. copy the reference tree to the scratch directory;
   2. stub `numba` (only `njit` is used, src/autopartition.py:76) so that the
      reference's test module imports;
   3. build the MKL stand-in of oracle/mkl_standin (plain CSR loop behind
@@ -21,14 +23,21 @@ Steps (harness shims only, all inside a scratch copy under /tmp):
      (src/consts.py:6) and run it under `ulimit -s unlimited`;
   7. run the reference's synthetic matrix generator (vbr_matrix_gen,
      synthesize_matrices/vbr_matrices_gen.py:36-113) after random.seed(s)
-     and store the arrays of the .vbr file it writes.
+     and store the arrays of the .vbr file it writes;
+  8. run the reference's partitioning steps, cut_indices2 with similarity2
+     and with similarity2_numba (src/autopartition.py:34-107) and
+     convert_sparse_to_vbr (utils/convert_real_to_vbr.py:98-199), on the
+     seeded matrices of synth.PARTITION_CASES, and cut_indices2 on the
+     MatrixMarket files of its manual_mtx/ directory (stored: the cuts, the
+     VBR index arrays and a sha256 of each file, not the matrices).
 The fixtures store the reference's inputs (or the seeds that regenerate
-them, with a sha256 of the arrays) and the printed outputs.
+them, with a sha256 of the arrays) and its outputs.
 
-    python tests/golden/make_golden.py --generator-only [/root/reference]
+    python tests/golden/make_golden.py --generator-only <reference root>
+    python tests/golden/make_golden.py --partition-only <reference root>
 
-adds (or refreshes) only the generator cases of step 7 in the existing
-fixture files.
+add (or refresh) only the cases of step 7 / step 8 in the existing fixture
+files.
 """
 from __future__ import annotations
 
@@ -41,6 +50,7 @@ import re
 import shutil
 import subprocess
 import sys
+import tempfile
 import types
 
 import numpy as np
@@ -48,7 +58,7 @@ import numpy as np
 REPO = pathlib.Path(__file__).resolve().parents[2]
 sys.path.insert(0, str(REPO))
 OUT = pathlib.Path(__file__).resolve().parent
-SCRATCH = pathlib.Path("/tmp/sable_ref_golden")
+SCRATCH = None   # the scratch copy of the reference (prepare)
 
 
 def sha(*arrays) -> str:
@@ -60,9 +70,16 @@ def sha(*arrays) -> str:
     return h.hexdigest()
 
 
+def reference_root(argv_root=None) -> pathlib.Path:
+    root = argv_root or os.environ.get("SABLE_REFERENCE_ROOT")
+    if not root:
+        sys.exit("name the reference root as the argument or in SABLE_REFERENCE_ROOT")
+    return pathlib.Path(root)
+
+
 def prepare(ref_root: pathlib.Path):
-    if SCRATCH.exists():
-        shutil.rmtree(SCRATCH)
+    global SCRATCH
+    SCRATCH = pathlib.Path(tempfile.mkdtemp(prefix="sable_ref_golden_")) / "ref"
     shutil.copytree(ref_root, SCRATCH, ignore=shutil.ignore_patterns(".git"))
     for p in SCRATCH.rglob("*"):
         try:
@@ -209,23 +226,75 @@ def write(fixtures):
     print("wrote", OUT / "golden.npz", "cases:", ", ".join(fixtures))
 
 
-def generator_only(ref_root="/root/reference"):
-    """Refresh only the step-7 cases in the existing fixture files."""
+def partition_cases(fixtures, ref_root: pathlib.Path):
+    """Step 8: the reference's partitioning steps on the seeded partition
+    matrices and on its manual_mtx files."""
+    import scipy.io
+    import scipy.sparse
+    from sable_gb300 import synth
+    ap = importlib.import_module("src.autopartition")
+    conv = importlib.import_module("utils.convert_real_to_vbr")
+    out_dir = SCRATCH / "_part"
+    out_dir.mkdir(exist_ok=True)
+
+    def run(name, A, meta, store_val):
+        csc = scipy.sparse.csc_matrix(A)
+        col, row = ap.cut_indices2(csc, 0.2, ap.similarity2)
+        col_n, row_n = ap.cut_indices2(csc, 0.2, ap.similarity2_numba)
+        f = {"kind": "partition", **meta, "col": np.asarray(col, np.int64), "row": np.asarray(row, np.int64),
+             "col_numba": np.asarray(col_n, np.int64), "row_numba": np.asarray(row_n, np.int64)}
+        try:
+            val, indx, bindx, bpntrb, bpntre = conv.convert_sparse_to_vbr(csc, row, col, name, str(out_dir))
+            f.update(vbr_ok=True, val_sha=sha(np.asarray(val, np.float64)), indx=np.asarray(indx, np.int64),
+                     bindx=np.asarray(bindx, np.int64), bpntrb=np.asarray(bpntrb, np.int64),
+                     bpntre=np.asarray(bpntre, np.int64))
+            if store_val:
+                f["val"] = np.asarray(val, np.float64)
+        except AssertionError:
+            f["vbr_ok"] = False   # a block row without stored blocks: the reference asserts
+        fixtures[name] = f
+
+    for case in synth.PARTITION_CASES:
+        A = synth.partition_case(*case)
+        run(f"part_{case[0]}", A, {"case": list(case), "sha": sha(A.indptr, A.indices, A.data)}, True)
+    for path in sorted((ref_root / "manual_mtx").glob("*.mtx")):
+        data = path.read_bytes()
+        A = scipy.io.mmread(str(path))
+        run(f"mtx_{path.stem}", A, {"file": f"manual_mtx/{path.name}",
+                                    "file_sha": hashlib.sha256(data).hexdigest()}, False)
+
+
+def _load_existing(drop_prefix):
     index = json.loads((OUT / "golden.json").read_text())
     with np.load(OUT / "golden.npz") as z:
         stored = {k: z[k] for k in z.files}
-    fixtures = {name: dict(meta) for name, meta in index.items() if not name.startswith("vbrgen_")}
+    fixtures = {name: dict(meta) for name, meta in index.items() if not name.startswith(drop_prefix)}
     for key, v in stored.items():
         name, field = key.split("__", 1)
         if name in fixtures:
             fixtures[name][field] = v
-    prepare(pathlib.Path(ref_root))
+    return fixtures
+
+
+def generator_only(ref_root=None):
+    """Refresh only the step-7 cases in the existing fixture files."""
+    fixtures = _load_existing("vbrgen_")
+    prepare(reference_root(ref_root))
     generator_cases(fixtures)
     write(fixtures)
 
 
-def main(ref_root="/root/reference"):
-    ref_root = pathlib.Path(ref_root)
+def partition_only(ref_root=None):
+    """Refresh only the step-8 cases in the existing fixture files."""
+    root = reference_root(ref_root)
+    fixtures = {k: v for k, v in _load_existing("part_").items() if not k.startswith("mtx_")}
+    prepare(root)
+    partition_cases(fixtures, root)
+    write(fixtures)
+
+
+def main(ref_root=None):
+    ref_root = reference_root(ref_root)
     from sable_gb300 import synth
     prepare(ref_root)
     fixtures = {}
@@ -276,11 +345,14 @@ def main(ref_root="/root/reference"):
         spmm_case(f"spmm400_N{N}_d{dens}", (s.val.astype(np.float64), *s.arrays()[1:]), X, dens, fixtures, meta)
 
     generator_cases(fixtures)
+    partition_cases(fixtures, ref_root)
     write(fixtures)
 
 
 if __name__ == "__main__":
     if sys.argv[1:2] == ["--generator-only"]:
         generator_only(*sys.argv[2:])
+    elif sys.argv[1:2] == ["--partition-only"]:
+        partition_only(*sys.argv[2:])
     else:
         main(*sys.argv[1:])

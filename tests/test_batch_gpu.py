@@ -132,3 +132,36 @@ def test_batch_argument_checks(cuda):
     import torch
     with pytest.raises(ValueError):
         b.run([torch.zeros(3, device="cuda")], [torch.zeros(m.n_rows, device="cuda")])
+
+
+def test_batch_256_generator_distribution(cuda):
+    """40 matrices from the 256-matrix batch workload's generator (rows
+    log-uniform in [1000, 20000], partitions U[4,128], block p = 0.02, SpMM
+    width 64 for every second matrix), each with the learned block choice at
+    its width, SpMM units in split BF16 (three terms), all in one CUDA-graph
+    launch; every output against the FP64 oracle."""
+    import torch
+    from sable_gb300 import blockmodel
+    mats, widths = synth.batch_256(count=40)
+    model = blockmodel.MLPModel.load()
+    plans, comps, xs = [], [], []
+    rng = np.random.default_rng(256)
+    for m, w in zip(mats, widths):
+        bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+        dense = model.choose_dense(convert.block_features(m.val, bt, w))
+        comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense, bt=bt)
+        comps.append(comp)
+        plans.append(Plan(comp, spmm_tc="split3", split_layout="mixed" if w == 1 else "separate"))
+        xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
+    b = Batch(plans, widths, use_graph=True)
+    ys = b.outputs()
+    b.run(xs, ys)
+    b.check()
+    worst = 0.0
+    for k, (m, comp, w, x, y) in enumerate(zip(mats, comps, widths, xs, ys)):
+        xn = x.cpu().numpy()
+        yr, ya = oracle.spmv_vbrc(comp, xn) if w == 1 else oracle.spmm_vbr(m, xn)
+        r = oracle.report(y.cpu().numpy(), yr, ya)
+        assert r["pass"], (k, w, r)
+        worst = max(worst, r["max"])
+    assert worst <= oracle.TOL

@@ -103,3 +103,18 @@ def test_spmm_50k_shape_sample(cuda):
     dense = convert.block_density_pct(convert.block_nnz(m.val, bt), bt) > 30
     _, r = run(m, dense, X, "split3", "umma", chunk_bytes=262144, split_layout="separate", row_tile=128)
     assert r["pass"], r
+
+
+@pytest.mark.parametrize("N", [32, 128])
+def test_spmm_50k_full_size(cuda, N):
+    """The full 50000^2 SpMM workload (1000 x 1000 partitions of 20..80, block
+    p = 0.01, 60 % dense blocks) at N = 32 and 128, with the learned block
+    choice and the entry point's launch shape, against the FP64 oracle on
+    every output."""
+    from sable_gb300 import blockmodel
+    m = synth.spmm_50k()
+    bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+    dense = blockmodel.MLPModel.load().choose_dense(convert.block_features(m.val, bt, N))
+    X = synth.dense_operand(m.n_cols, N, 7)
+    _, r = run(m, dense, X, "split3", "umma", chunk_bytes=262144, split_layout="separate", row_tile=128)
+    assert r["pass"] and r["rows"] == m.n_rows * N, r
