@@ -24,9 +24,13 @@ out, inside the timed region).  Also reported, each timed the same way:
   batch_256  256 matrices (half SpMV, half SpMM N = 64): plain = reference
              choice, one launch per matrix, FP32; learned+batched = MLP
              choice, one persistent-kernel graph launch
-`--impl reference` times the reference's CPU executor (the oracle's C port
-of its generated code, built with its compiler flags, FP64, all host cores)
-on the headline workload.  Under torchrun each rank runs its own seeded
+`--impl reference` times the reference's CPU executor on the headline
+workload: its own generated C (oracle/refc.py: gen_multi_threaded_spmv,
+FP64, OpenMP over the host cores, its compiler flags; about four minutes of
+compilation the first time on a host), or, where those sources were not
+generated, the oracle's C port of it.  The GPU arm's cpu_baseline reports the
+same program when it is already compiled on the host, else the port, for
+the same number of iterations.  Under torchrun each rank runs its own seeded
 replica (weak scaling, no collective on the data path).
 """
 from __future__ import annotations
@@ -410,7 +414,7 @@ def run_sable(args):
         out["spmm_50k"] = bench_spmm(10, flush)
         out["batch_256"] = bench_batch(10)
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(m, bt, plain_choice, x, B, seconds=args.cpu_seconds)
+        out["cpu_baseline"] = cpu_baseline(m, bt, plain_choice, x, B, args.steps)
     if rank == 0:
         print(json.dumps(out))
     learned.close()
@@ -420,21 +424,47 @@ def run_sable(args):
         dist.destroy_process_group()
 
 
-def cpu_baseline(m, bt, choice, x, B, seconds: float = 15.0, threads: int | None = None) -> dict:
-    """The reference's generated SpMV executor, as the oracle's C port (FP64,
-    its own block choice, its compiler flags), on the host cores."""
+def reference_c(steps: int, compile_ok: bool):
+    """The reference's own generated SpMV program for this workload (its
+    multi-threaded form, OpenMP over the host cores; oracle/refc.py), run for
+    `steps` timed iterations, or None when its sources are absent (or, with
+    compile_ok False, when it is not compiled on this host yet).  Also returns
+    its error against the FP64 oracle."""
+    from oracle import oracle, refc
+    if not refc.generated() or (not compile_ok and not refc.compiled(("mt",))):
+        return None
+    r = refc.run(steps, kinds=("mt",))["mt"]
+    m, x, comp = refc._workload()
+    y, ya = oracle.spmv_vbrc(comp, x)
+    rep = oracle.report(r["y"], y, ya, 1e-10)
+    return r, rep
+
+
+def cpu_baseline(m, bt, choice, x, B, steps: int) -> dict:
+    """The reference's CPU executor on the host cores, `steps` iterations:
+    its own generated C when compiled on this host (see reference_c), else
+    the oracle's C port of it (FP64, its block choice, its compiler flags)."""
+    ref = reference_c(steps, compile_ok=False)
+    if ref is not None:
+        r, rep = ref
+        t = np.asarray(r["times_ns"], np.float64) * 1e-9
+        return {"value": round(B / float(np.mean(t)) / 1e9, 3), "unit": "GB/s", "cores": int(r["threads"]),
+                "kind": "reference",
+                "sample": f"full 100000^2 matrix, {len(t)} SpMV iterations (mean) of the reference's generated "
+                          f"multi-threaded C (its CFLAGS, MKL stand-in for its CSR part), FP64, its block choice; "
+                          f"max error vs FP64 oracle {rep['max']:.1e} of |A||x|"}
     from oracle import oracle
     from sable_gb300 import convert
     comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, choice, bt=bt,
                             value_dtype=np.float64)
-    threads = threads or os.cpu_count() or 1
-    t, used, _ = oracle.cpu_spmv_timed(comp, x, threads, 2)  # warm-up, sizes the sample
-    per = max(float(np.median(t)) * 1e-9, 1e-4)
-    iters = int(max(3, min(200, seconds / per)))
-    t, used, _ = oracle.cpu_spmv_timed(comp, x, threads, iters)
-    med = float(np.median(t)) * 1e-9
-    return {"value": round(B / med / 1e9, 3), "unit": "GB/s", "cores": int(used), "kind": "port",
-            "sample": f"full 100000^2 matrix, {iters} SpMV iterations (median), FP64, reference block choice"}
+    threads = os.cpu_count() or 1
+    oracle.cpu_spmv_timed(comp, x, threads, 2)
+    t, used, _ = oracle.cpu_spmv_timed(comp, x, threads, steps)
+    return {"value": round(B / (float(np.mean(t)) * 1e-9) / 1e9, 3), "unit": "GB/s", "cores": int(used),
+            "kind": "port",
+            "sample": f"full 100000^2 matrix, {steps} SpMV iterations (mean), FP64, reference block choice "
+                      f"(the oracle's C port of the generated executor; the reference's own generated C is not "
+                      f"compiled on this host)"}
 
 
 def run_reference(args):
@@ -445,21 +475,34 @@ def run_reference(args):
     from oracle import oracle
     from sable_gb300 import blockmodel, convert
     m, x, bt, nnz, B = build_workload(0)
-    plain_choice = blockmodel.RFTableModel().choose_dense(convert.block_features(m.val, bt, 1))
-    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, plain_choice, bt=bt,
-                            value_dtype=np.float64)
-    threads = os.cpu_count() or 1
-    oracle.cpu_spmv_timed(comp, x, threads, max(1, args.warmup))
-    t, used, _ = oracle.cpu_spmv_timed(comp, x, threads, args.steps)
-    ms = float(np.mean(t)) * 1e-6
+    ref = reference_c(args.steps, compile_ok=True)
+    if ref is not None:
+        r, rep = ref
+        t = np.asarray(r["times_ns"], np.float64) * 1e-9
+        ms = float(np.mean(t)) * 1e3
+        kind, used = "reference", int(r["threads"])
+        sample = (f"full matrix, {len(t)} timed SpMV iterations of the reference's own generated multi-threaded C "
+                  f"(gen_multi_threaded_spmv, {used} OpenMP sections, its CFLAGS for this host, MKL stand-in for "
+                  f"its CSR part; its first iteration dropped as it does); max error vs FP64 oracle "
+                  f"{rep['max']:.1e} of |A||x|")
+    else:
+        plain_choice = blockmodel.RFTableModel().choose_dense(convert.block_features(m.val, bt, 1))
+        comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, plain_choice, bt=bt,
+                                value_dtype=np.float64)
+        threads = os.cpu_count() or 1
+        oracle.cpu_spmv_timed(comp, x, threads, max(1, args.warmup))
+        t, used, _ = oracle.cpu_spmv_timed(comp, x, threads, args.steps)
+        ms = float(np.mean(t)) * 1e-6
+        kind = "port"
+        sample = f"full matrix, {args.steps} timed SpMV iterations after {args.warmup} warm-up (oracle C port)"
     value = B / (ms * 1e-3) / 1e9
     out = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; no dataset)",
         "config": {"workload": WORKLOAD, "choice": "reference RandomForest", "bytes_per_step": int(B)},
-        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": int(used), "kind": "port",
-                         "sample": f"full matrix, {args.steps} timed SpMV iterations after {args.warmup} warm-up"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": int(used), "kind": kind,
+                         "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out))
@@ -473,7 +516,6 @@ def main():
     ap.add_argument("--impl", default="sable", choices=["sable", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--quick", action="store_true", help="headline SpMV only (no SpMM / batch sections)")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--spmm-profile", help="N,ROW_TILE,CHUNK_BYTES: only run the 50000^2 SpMM (learned choice, "
                                            "split BF16) in this shape, for kernel profiles")
     ap.add_argument("--shape", help="ROW_TILE,CHUNK_BYTES: run the headline on the per-warp executor in this shape "
