@@ -31,7 +31,9 @@ compilation the first time on a host), or, where those sources were not
 generated, the oracle's C port of it.  The GPU arm's cpu_baseline reports the
 same program when it is already compiled on the host, else the port, for
 the same number of iterations.  Under torchrun each rank runs its own seeded
-replica (weak scaling, no collective on the data path).
+replica (weak scaling, no collective on the data path); with --strong the
+ranks instead take block-row shards of the one matrix, balanced by algorithmic
+bytes (sable_gb300.shard), each writing its own rows of y (strong scaling).
 """
 from __future__ import annotations
 
@@ -335,7 +337,17 @@ def run_sable(args):
     from sable_gb300.plan import Plan
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
-    m, x, bt, nnz, B = build_workload(rank)
+    if args.strong and world > 1:
+        from sable_gb300 import metrics, shard
+        m_full, x, _, _, B_job = build_workload(0)
+        a0, a1 = shard.shard_block_rows(m_full, world)[rank]
+        m = shard.sub_block_rows(m_full, a0, a1)
+        bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+        nnz = convert.block_nnz(m.val, bt)
+        B = metrics.spmv_matrix_bytes(bt, nnz) + 4 * (m.n_rows + m.n_cols)
+    else:
+        m, x, bt, nnz, B = build_workload(rank)
+        B_job = world * B
     feats, plain_choice, learned_choice = choices(m, bt, 1)
     comp_l = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, learned_choice, bt=bt)
     comp_p = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, plain_choice, bt=bt)
@@ -352,10 +364,15 @@ def run_sable(args):
     with ClockSampler(local) as clk:
         t_learn = time_device(lambda: learned.run(xd, yd), args.steps, args.warmup, world, flush)
     t_plain = time_device(lambda: plain.spmv(xd, yd), args.steps, args.warmup, world, flush)
+    # block choice alone: the reference's RandomForest choice in the learned form's launch shape
+    rf_same = autotune._build(comp_p, learned.config, 1, None)
+    t_rf_same = time_device(lambda: rf_same.run(xd, yd), args.steps, args.warmup, world, flush)
+    rf_same.close()
+    ms_rf_same = max_over_ranks(statistics.mean(t_rf_same), world)
     ms = max_over_ranks(statistics.mean(t_learn), world)
     ms_plain = max_over_ranks(statistics.mean(t_plain), world)
-    value = world * B / (ms * 1e-3) / 1e9
-    value_plain = world * B / (ms_plain * 1e-3) / 1e9
+    value = B_job / (ms * 1e-3) / 1e9
+    value_plain = B_job / (ms_plain * 1e-3) / 1e9
 
     # end to end through the C ABI with host buffers (pinned), learned plan
     xh = torch.as_tensor(x).pin_memory()
@@ -388,32 +405,37 @@ def run_sable(args):
         traffic = int(hit.group(1)) if hit else None
     out = {
         "metric": METRIC, "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; no dataset)",
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True,
+        "scaling": "strong" if args.strong and world > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded; no dataset)",
         "config": {"workload": WORKLOAD, "l2": "flushed between timed steps (256 MB write, then 256 MB read of a "
                                                "clean buffer so no dirty lines are written back inside the step)",
                    "choice": "learned MLP cost model (sable_gb300/models/block_cost_mlp.npz)",
                    "launch_shape": learned.config, "n_blocks": int(m.n_blocks), "stored_values": int(len(m.val)),
                    "nnz": int(nnz.sum()), "bytes_per_step": int(B), "dense_frac": round(float(learned_choice.mean()), 4),
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": (f"block-row shards x{world}" if args.strong and world > 1
+                                   else f"replicas x{world}")},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": traffic,
                      "peak_source": pk["source"],
                      "kernel": kernel + ("" if learned.launches_per_run() == 1 else " + spmv_combine_kernel")},
-        "e2e": {"value": round(world * B / e2e_s / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * m.n_cols,
+        "e2e": {"value": round(B_job / e2e_s / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": 4 * m.n_cols,
                 "d2h_bytes_per_step": 4 * m.n_rows},
         "gpu_launches": args.steps * learned.launches_per_run(),
         "plain": {"value": round(value_plain, 2), "unit": "GB/s", "ms_per_step": round(ms_plain, 5),
                   "choice": "reference RandomForest (models/density_threshold_spmv.pkl)",
                   "frac": round(B / (statistics.mean(t_plain) * 1e-3) / 1e9 / pk["hbm_gbs"], 4)},
         "learned_vs_plain": round(ms_plain / ms, 3),
+        "block_choice_only": {"rf_choice_same_shape_ms": round(ms_rf_same, 5),
+                              "learned_vs_rf_same_shape": round(ms_rf_same / ms, 3),
+                              "what": "MLP vs RandomForest block choice, both in the learned form's launch shape"},
         "autotune": learned.table,
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.quick:
         out["spmm_50k"] = bench_spmm(10, flush)
         out["batch_256"] = bench_batch(10)
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(m, bt, plain_choice, x, B, args.steps)
     if rank == 0:
         print(json.dumps(out))
@@ -515,6 +537,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="sable", choices=["sable", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--strong", action="store_true", help="under torchrun: shard the block rows of one matrix over the "
+                                                          "ranks (strong scaling) instead of one replica per rank")
     ap.add_argument("--quick", action="store_true", help="headline SpMV only (no SpMM / batch sections)")
     ap.add_argument("--spmm-profile", help="N,ROW_TILE,CHUNK_BYTES: only run the 50000^2 SpMM (learned choice, "
                                            "split BF16) in this shape, for kernel profiles")

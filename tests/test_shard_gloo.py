@@ -1,7 +1,12 @@
-"""Multi-rank host logic on CPU (gloo, world size 2): block-row shards of a
-VBR matrix computed by separate ranks and gathered give the full y; batch
-matrices are spread over ranks by cost.  The GPU path shards the same way,
-one plan per rank, with no collective on the data path."""
+"""Multi-rank host logic on CPU (gloo, world size 2): each rank takes its
+block-row shard of a VBR matrix (shard.shard_block_rows -> sub_block_rows),
+builds the work-item records the library would upload for that shard
+(sable_plan_layout_host, the records exactly as a plan on that rank's GPU
+holds them: the per-warp compact records of the headline executor and the
+standard per-CTA records), multiplies them in FP64 with the host decoder, and
+the gathered row slices give the full matrix's y from the FP64 oracle.
+Batch matrices are spread over ranks by cost.  The GPU path shards the same
+way, one plan per rank, with no collective on the data path."""
 import os
 import socket
 
@@ -12,6 +17,8 @@ import torch.multiprocessing as mp
 
 from oracle import oracle
 from sable_gb300 import convert, shard, synth
+
+from layout_decode import decode_multiply, layout
 
 
 def _matrix():
@@ -26,6 +33,13 @@ def _free_port():
     return port
 
 
+def _choice(n_blocks, seed=9):
+    return np.random.default_rng(seed).random(n_blocks) < 0.5
+
+
+SHAPES = ((2, 16, 32768, 0), (0, 64, 32768, 0), (0, 128, 8192, 1))   # schedule, row tile, item bytes, split layout
+
+
 def _rank(rank, world, port, out):
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
@@ -34,14 +48,26 @@ def _rank(rank, world, port, out):
     x = synth.vector(m.n_cols, 3)
     a0, a1 = shard.shard_block_rows(m, world)[rank]
     sub = shard.sub_block_rows(m, a0, a1)
-    dense = np.ones(sub.n_blocks, bool)
-    comp = convert.compress(sub.val.astype(np.float64), sub.rpntr, sub.cpntr, sub.indx, sub.bindx, sub.bpntrb,
-                            sub.bpntre, dense, value_dtype=np.float64)
-    y, _ = oracle.spmv_vbrc(comp, x) if sub.n_rows else (np.zeros(0), None)
+    # the block choice of the shard's blocks is the full matrix's choice for
+    # those blocks: the blocks of block rows [a0, a1) are one contiguous run
+    full = _choice(m.n_blocks)
+    firsts = [int(m.bpntrb[a]) for a in range(a0, a1) if m.bpntrb[a] != -1]
+    k0 = min(firsts) if firsts else 0
+    dense = full[k0:k0 + sub.n_blocks]
+    comp = convert.compress(sub.val, sub.rpntr, sub.cpntr, sub.indx, sub.bindx, sub.bpntrb, sub.bpntre, dense)
+    ys = []
+    for schedule, row_tile, chunk, split in SHAPES:
+        if sub.n_rows == 0:
+            ys.append(np.zeros(0))
+            continue
+        rec, off, byt = layout(comp, row_tile, chunk, schedule, split)
+        y, cover = decode_multiply(rec, off, byt, x, sub.n_rows, compact=schedule == 2)
+        assert np.all(cover == 1)
+        ys.append(y)
     parts = [None] * world
-    dist.all_gather_object(parts, np.asarray(y))   # uneven row slices
+    dist.all_gather_object(parts, ys)   # uneven row slices, one list per rank
     if rank == 0:
-        out.put(np.concatenate(parts))
+        out.put([np.concatenate([p[s] for p in parts]) for s in range(len(SHAPES))])
     dist.barrier()
     dist.destroy_process_group()
 
@@ -70,12 +96,13 @@ def test_two_ranks_gather_full_y():
     procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
     for p in procs:
         p.start()
-    y = q.get(timeout=120)
+    ys = q.get(timeout=300)
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
     m = _matrix()
-    comp = convert.compress(m.val.astype(np.float64), m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre,
-                            np.ones(m.n_blocks, bool), value_dtype=np.float64)
-    y_full, _ = oracle.spmv_vbrc(comp, synth.vector(m.n_cols, 3))
-    np.testing.assert_allclose(y, y_full, rtol=0, atol=1e-12)
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, _choice(m.n_blocks))
+    y_full, yabs = oracle.spmv_vbrc(comp, synth.vector(m.n_cols, 3))
+    for y in ys:
+        assert y.shape == y_full.shape
+        assert np.all(np.abs(y - y_full) <= 1e-12 * (yabs + 1.0))
