@@ -365,7 +365,7 @@ def run_sable(args):
         t_learn = time_device(lambda: learned.run(xd, yd), args.steps, args.warmup, world, flush)
     t_plain = time_device(lambda: plain.spmv(xd, yd), args.steps, args.warmup, world, flush)
     # block choice alone: the reference's RandomForest choice in the learned form's launch shape
-    rf_same = autotune._build(comp_p, learned.config, 1, None)
+    rf_same = autotune._build(comp_p, learned.config, 1, "off")
     t_rf_same = time_device(lambda: rf_same.run(xd, yd), args.steps, args.warmup, world, flush)
     rf_same.close()
     ms_rf_same = max_over_ranks(statistics.mean(t_rf_same), world)

@@ -84,8 +84,8 @@ spmv_items_kernel(const LaunchArgs a) {
 
 // ---------------------------------------------------------------------------
 // One warp per work item (schedule 2), over compact records.  The record is
-// read straight from HBM with coalesced streaming loads after one bulk L2
-// prefetch: no shared-memory staging of the record, no TMA wait and no CTA
+// read straight from HBM with coalesced streaming loads after a bulk L2
+// prefetch of its head: no shared-memory staging of the record, no TMA wait and no CTA
 // barrier, so every warp of the SM is an independent stream.  The item's x
 // window (panel columns, then the columns of its CSR entries) is gathered
 // once into shared memory from its column runs, so neither part waits on a
@@ -105,11 +105,19 @@ constexpr int WI_GU = 8;          // window positions per lane in flight while g
 
 __device__ __forceinline__ float4 ld_stream(const float4 *p) { return __ldcs(p); }
 
-// One bulk L2 prefetch of a whole record (16-byte aligned, a multiple of 16
-// bytes): DRAM sees one large request per item, and the warp's own loads of
-// the record hit L2 instead of each waiting a DRAM round trip.
+// One bulk L2 prefetch of the first bytes of a record (16-byte aligned, a
+// multiple of 16 bytes): the header, the window runs and the first panel
+// steps are in L2 by the time the warp asks for them.  Only the head: with
+// whole records prefetched, the first wave of warps put ~130 MB of requests
+// before DRAM at once, their headers waited behind them and the SMs took
+// about 5 us to reach full occupancy (1.5 us with an 8 KB head); the kernel
+// was 6 % slower on the 100000^2 workload.  Prefetching the rest later (after
+// the window gather, rolling ahead of the panel, or the next item's head) was
+// slower or no faster: the warps' own loads stream the body.
+constexpr int WI_PREFETCH_BYTES = 8192;
 __device__ __forceinline__ void prefetch_record(const unsigned char *R, int bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(R), "r"((unsigned)bytes) : "memory");
+    const unsigned n = (unsigned)min(bytes, WI_PREFETCH_BYTES);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(R), "r"(n) : "memory");
 }
 
 // The x window of a compact record into xw[0, nw).  Runs are taken 32 at a
@@ -624,12 +632,21 @@ int spmv_warp_smem(int stage_bytes, int xg_floats) {
     return SABLE_WSTAGES * stage_bytes + SABLE_WSTAGES * 4 * xg_floats + 4 * ROWBUF_FLOATS;
 }
 
+// Warp workers of the persistent SpMV per SM; 1 when the records are too
+// large for its ring (the plan then runs one CTA per item).  That refusal is
+// expected, so its error is taken off the runtime's last-error state, where
+// the next launch check would otherwise report it.
 int spmv_warp_workers_per_sm(int stage_bytes, int xg_floats) {
     const int smem = spmv_warp_smem(stage_bytes, (xg_floats + 3) & ~3);
-    if (cudaFuncSetAttribute(spmv_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(spmv_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
+        cudaGetLastError();
         return 1;
+    }
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, spmv_warp_kernel, 32, smem) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, spmv_warp_kernel, 32, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
     return n > 0 ? n : 1;
 }
 

@@ -118,3 +118,36 @@ def test_spmm_50k_full_size(cuda, N):
     X = synth.dense_operand(m.n_cols, N, 7)
     _, r = run(m, dense, X, "split3", "umma", chunk_bytes=262144, split_layout="separate", row_tile=128)
     assert r["pass"] and r["rows"] == m.n_rows * N, r
+
+
+@pytest.mark.parametrize("N", [36, 100, 132, 260])
+@pytest.mark.parametrize("tc", ["split2", "split3"])
+def test_widths_strides_and_the_entry_without_allocation(cuda, N, tc):
+    """Widths that are not multiples of 8 or of the N-slice width, X and Y
+    inside wider rows (leading dimensions above N): within the tolerance of
+    FP64, nothing written past column N of Y, and bit-identical to the entry
+    point without allocation, which runs the same kernel with its split-tile
+    scratch in the library's fixed array."""
+    import torch
+    from sable_gb300 import _lib
+    m = random_vbr(83, [40, 128, 7, 64, 100], [33, 128, 16, 90, 5], 0.8, dense_frac=0.8)
+    dense = np.random.default_rng(84).random(m.n_blocks) < 0.8
+    comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense)
+    plan = Plan(comp, spmm_tc=tc, tc_kernel="umma")
+    Xw = torch.as_tensor(synth.dense_operand(m.n_cols, N + 12, 85)).cuda()
+    X = Xw[:, :N]                      # leading dimension N + 12
+    Yw = torch.full((m.n_rows, N + 8), float("nan"), device="cuda")
+    Y = Yw[:, :N]
+    plan.spmm(X, Y)
+    Yn = torch.full((m.n_rows, N), float("nan"), device="cuda")
+    lib = _lib.load()
+    _lib.check(lib.sable_spmm_noalloc(plan.handle, X.data_ptr(), X.stride(0), Yn.data_ptr(), N, N,
+                                      torch.cuda.current_stream().cuda_stream), "sable_spmm_noalloc")
+    plan.check()
+    Yh = Y.cpu().numpy()
+    assert np.array_equal(Yh, Yn.cpu().numpy())
+    assert torch.isnan(Yw[:, N:]).all()          # nothing written past N
+    Yr, Ya = oracle.spmm_vbr(m, X.cpu().numpy())
+    r = oracle.report(Yh, Yr, Ya, oracle.TOL_SPLIT2 if tc == "split2" else oracle.TOL)
+    assert r["pass"], r
+    plan.close()
