@@ -189,7 +189,7 @@ def time_device(fn, steps: int, warmup: int, world: int, flush):
     return [s.elapsed_time(e) for s, e in evs]
 
 
-def bench_spmm(reps: int, flush) -> dict:
+def bench_spmm(reps: int, flush, cpu: bool = True) -> dict:
     """50000^2 SpMM at N = 32 and 128: plain FP32 vs learned split-BF16 (autotuned)."""
     import scipy.sparse
     import torch
@@ -237,12 +237,28 @@ def bench_spmm(reps: int, flush) -> dict:
             "error_vs_fp64_scaled": {"max": float(rel.max()), "median": float(np.median(rel)), "rows": 4000,
                                      "precision": "split-BF16, three terms (hi+mid+lo), six products, FP32 accum"},
             "dense_frac_learned": round(float(mlp.mean()), 3), "dense_frac_plain": round(float(rf.mean()), 3)}
+        if cpu:
+            out[f"N{N}"]["cpu_baseline"] = cpu_spmm_baseline(m, X.cpu().numpy(), F)
         plain.close()
         tuned.close()
     return out
 
 
-def bench_batch(reps: int) -> dict:
+def cpu_spmm_baseline(m, Xh, F) -> dict:
+    """The oracle's C port of the reference's generated SpMM executor
+    (gen_multi_threaded_spmm: FP32, i-j-k loops per dense block, block rows
+    split over the host cores by LPT), its compiler flags, the full matrix."""
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    oracle.cpu_spmm_timed(m, Xh, 0, threads, 1)
+    t, used, _ = oracle.cpu_spmm_timed(m, Xh, 0, threads, 3)
+    ms = float(np.mean(t)) * 1e-6
+    return {"value": round(F / (ms * 1e-3) / 1e9, 1), "unit": "GFLOP/s", "ms": round(ms, 3), "cores": int(used),
+            "kind": "port", "sample": f"full matrix, 3 timed SpMM iterations after one warm-up, width {Xh.shape[1]} "
+                                      f"(the oracle's C port of the generated multi-threaded SpMM, FP32)"}
+
+
+def bench_batch(reps: int, cpu: bool = True) -> dict:
     """256 mixed matrices: per-matrix launches (plain) vs one batched graph launch (learned)."""
     import torch
     from sable_gb300 import autotune, convert, synth
@@ -292,6 +308,28 @@ def bench_batch(reps: int) -> dict:
     for p in plain + learned:
         p.close()
     batch.close()
+    cpu_b = None
+    if cpu:
+        # the oracle's C ports of the generated executors, one matrix after the
+        # other (the reference runs one generated program per matrix), the
+        # reference's block choice, all host cores per matrix
+        threads, tot_ns, used = os.cpu_count() or 1, 0.0, 1
+        for m, w, x in zip(mats, widths, xs):
+            xn = x.cpu().numpy()
+            if w == 1:
+                bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+                _, rf, _ = choices(m, bt, 1)
+                comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, rf, bt=bt,
+                                        value_dtype=np.float64)
+                t, used, _ = oracle.cpu_spmv_timed(comp, xn, threads, 3)
+            else:
+                t, used, _ = oracle.cpu_spmm_timed(m, xn, 0, threads, 3)
+            tot_ns += float(np.mean(t))
+        cpu_ms = tot_ns * 1e-6
+        cpu_b = {"value": round(2 * nnz_work / (cpu_ms * 1e6), 1), "unit": "GFLOP/s", "ms": round(cpu_ms, 3),
+                 "cores": int(used), "kind": "port",
+                 "sample": "all 256 matrices, sum over matrices of the mean of 3 timed iterations (the oracle's C ports "
+                           "of the generated SpMV (FP64) and SpMM (FP32) executors, the reference block choice)"}
     return {"workload": "batch_256: 256 square matrices n log-U[1000,20000], partitions U[4,128], block p=0.02, "
                         "dense fraction U[0.2,0.8], sparse density U[0.02,0.4]; SpMM N=64 for half",
             "plain_ms": round(ms_p, 4), "plain_launches": len(mats) + sum(1 for w in widths if w == 1),
@@ -301,7 +339,8 @@ def bench_batch(reps: int) -> dict:
                                      "matrices": len(errs), "tolerance": oracle.TOL,
                                      "measure": "per output |y - y_fp64| / (|A||x|), all 256 matrices"},
             "batch": {"n_units": info["n_units"], "n_ctas": info["n_ctas"], "stages": info["stages"],
-                      "graph": True, "tuning": table}}
+                      "graph": True, "tuning": table},
+            "cpu_baseline": cpu_b}
 
 
 def run_spmm_profile(args):
@@ -433,8 +472,8 @@ def run_sable(args):
         "clocks": clk.summary(),
     }
     if rank == 0 and not args.quick:
-        out["spmm_50k"] = bench_spmm(10, flush)
-        out["batch_256"] = bench_batch(10)
+        out["spmm_50k"] = bench_spmm(10, flush, cpu=not args.no_cpu_baseline)
+        out["batch_256"] = bench_batch(10, cpu=not args.no_cpu_baseline)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(m, bt, plain_choice, x, B, args.steps)
     if rank == 0:
