@@ -321,9 +321,10 @@ def bench_batch(reps: int, cpu: bool = True) -> dict:
                 _, rf, _ = choices(m, bt, 1)
                 comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, rf, bt=bt,
                                         value_dtype=np.float64)
-                t, used, _ = oracle.cpu_spmv_timed(comp, xn, threads, 3)
+                t, u, _ = oracle.cpu_spmv_timed(comp, xn, threads, 3)
             else:
-                t, used, _ = oracle.cpu_spmm_timed(m, xn, 0, threads, 3)
+                t, u, _ = oracle.cpu_spmm_timed(m, xn, 0, threads, 3)
+            used = max(used, int(u))   # small matrices split over fewer threads
             tot_ns += float(np.mean(t))
         cpu_ms = tot_ns * 1e-6
         cpu_b = {"value": round(2 * nnz_work / (cpu_ms * 1e6), 1), "unit": "GFLOP/s", "ms": round(cpu_ms, 3),

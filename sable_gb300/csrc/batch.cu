@@ -12,7 +12,12 @@
 // queue order from an atomic head, so the largest units start first and the
 // small ones fill the tail (greedy list scheduling).
 //
-// SpMM units run the bodies of spmm_item.cuh from global memory.  SpMV units
+// Split-BF16 SpMM items of plans that hold tcgen05 panel terms (the default
+// for plans built with spmm_tc) do not enter the queue: they run on the
+// tcgen05 kernel (spmm_umma.cu), one launch per N-slice width over the items
+// of all such matrices (largest first, each CTA reading its matrix from the
+// batch's matrix table), before the persistent kernel, in the same graph.
+// The other SpMM units run the bodies of spmm_item.cuh from global memory.  SpMV units
 // run the CTA-per-item body (spmv_item.cuh) from an S-stage TMA ring that
 // keeps S claimed records in flight per CTA (S = 2..8; by default the
 // deepest ring that still allows the most CTAs per SM).  A CTA's shared memory is used by one
@@ -205,6 +210,13 @@ __global__ void patch_mat_kernel(unsigned char *records, const ItemRef *items, c
 
 int spmm_nt(int N) { return N <= 16 ? 16 : N <= 32 ? 32 : 64; }
 
+// A split-BF16 SpMM matrix whose plan holds tcgen05 panel terms runs on the
+// tcgen05 kernel, outside the persistent kernel's queue.
+bool runs_umma(const sable_plan *p, int W) {
+    return W >= 32 && p->spmm_tc && p->tc_kernel == SABLE_TC_KERNEL_UMMA && p->d_umma &&
+           p->umma_off_host.size() == (size_t)p->n_items;
+}
+
 int16_t spmm_kind(int nt, int tc_terms) {
     if (tc_terms == 0) return nt == 16 ? U_F32_16 : nt == 32 ? U_F32_32 : U_F32_64;
     if (tc_terms == 2) return nt == 32 ? U_TC2_32 : U_TC2_64;
@@ -239,8 +251,19 @@ BatchKernel batch_kernel_for(int S, bool spmm) {
 
 }  // namespace
 
+// Split-BF16 SpMM items run by the tcgen05 kernel, per N-slice width and
+// number of terms.
+struct UmmaGroup {
+    int nt = 0, terms = 0, N = 0, hp = 16;
+    int n_items = 0;
+    ItemRef *d_items = nullptr;     // merged records, largest first
+    int64_t *d_off = nullptr;       // byte offset of each item's panel terms in d_umma, -1: none
+};
+
 struct sable_batch {
     int device = 0;
+    std::vector<UmmaGroup> umma;
+    unsigned char *d_umma = nullptr;     // merged tcgen05 panel terms
     int n_mats = 0;
     std::vector<int32_t> width;
     std::vector<int64_t> n_rows, n_cols;
@@ -258,6 +281,7 @@ struct sable_batch {
     SplitTile *d_splits = nullptr;       // SpMV split tiles of every matrix (combine launch)
     int n_splits = 0;
     int64_t n_units = 0, device_bytes = 0;
+    int64_t n_queue = 0;                 // units of the persistent kernel's queue (n_units adds the tcgen05 ones)
     int stage_bytes = 0, smem = 0, n_ctas = 0, stages = 0;
     BatchKernel kernel = nullptr;
     bool mats_valid = false;
@@ -281,13 +305,30 @@ int batch_launch(sable_batch *bt, cudaStream_t s) {
     a.mats = bt->d_mats;
     a.head = bt->d_head;
     a.error = bt->d_error;
-    a.n_units = (int)bt->n_units;
+    a.n_units = (int)bt->n_queue;
     a.stage_bytes = bt->stage_bytes;
-    cudaError_t e = cudaMemsetAsync(bt->d_head, 0, sizeof(int), s);
-    if (e != cudaSuccess) return cuda_fail(e, "batch queue reset");
-    bt->kernel<<<bt->n_ctas, SABLE_THREADS, bt->smem, s>>>(a);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "batch kernel launch");
+    for (const UmmaGroup &g : bt->umma) {
+        LaunchArgs la;
+        memset(&la, 0, sizeof la);
+        la.records = bt->d_records;
+        la.items = g.d_items;
+        la.mats = bt->d_mats;
+        la.umma = bt->d_umma;
+        la.umma_off = g.d_off;
+        la.umma_hp = g.hp;
+        la.error = bt->d_error;
+        la.n_items = g.n_items;
+        const int ec = launch_spmm_umma(la, g.N, g.nt, g.terms, 0, false, s);
+        if (ec) return cuda_fail((cudaError_t)ec, "batch tcgen05 SpMM launch");
+    }
+    cudaError_t e = cudaSuccess;
+    if (bt->n_queue > 0) {
+        e = cudaMemsetAsync(bt->d_head, 0, sizeof(int), s);
+        if (e != cudaSuccess) return cuda_fail(e, "batch queue reset");
+        bt->kernel<<<bt->n_ctas, SABLE_THREADS, bt->smem, s>>>(a);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return cuda_fail(e, "batch kernel launch");
+    }
     if (bt->n_splits > 0) {
         MatIO none;
         memset(&none, 0, sizeof none);
@@ -329,6 +370,11 @@ int sable_batch_destroy(sable_batch *bt) {
     cudaFree(bt->d_head);
     cudaFree(bt->d_error);
     cudaFree(bt->d_splits);
+    for (UmmaGroup &g : bt->umma) {
+        cudaFree(g.d_items);
+        cudaFree(g.d_off);
+    }
+    cudaFree(bt->d_umma);
     if (bt->h_mats) cudaFreeHost(bt->h_mats);
     if (prev >= 0) cudaSetDevice(prev);
     delete bt;
@@ -388,15 +434,41 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     std::vector<Sortable> q;
     int64_t partial_total = 0, counter_total = 0, rec_base = 0;
     std::vector<int64_t> part_off(n_plans), cnt_off(n_plans);
+    // tcgen05 items per (slice width, terms): merged item, panel-term offset, cost
+    struct UmmaItem {
+        ItemRef r;
+        int64_t off;
+    };
+    std::vector<UmmaGroup> groups;
+    std::vector<std::vector<UmmaItem>> group_items;
+    int64_t umma_base = 0;
     for (int i = 0; i < n_plans; ++i) {
         const sable_plan *p = plans[i];
         const int W = widths[i];
         bt->width.push_back(W);
         bt->n_rows.push_back(p->n_rows);
         bt->n_cols.push_back(p->n_cols);
-        const int nt = W == 1 ? 1 : spmm_nt(W);
-        const int slices = W == 1 ? 1 : (W + nt - 1) / nt;
         const int terms = (W >= 32 && p->spmm_tc) ? (p->spmm_tc == SABLE_TC_SPLIT3 ? 3 : 2) : 0;
+        // split-BF16 SpMM of a plan with tcgen05 panel terms: the tcgen05
+        // kernel, with the slice width of sable_spmm
+        const bool umma = terms && runs_umma(p, W);
+        const int nt = W == 1 ? 1 : umma ? spmm_slice_width(W) : spmm_nt(W);
+        const int slices = W == 1 ? 1 : (W + nt - 1) / nt;
+        int gidx = -1;
+        if (umma) {
+            for (size_t g = 0; g < groups.size(); ++g)
+                if (groups[g].nt == nt && groups[g].terms == terms) gidx = (int)g;
+            if (gidx < 0) {
+                UmmaGroup g;
+                g.nt = nt;
+                g.terms = terms;
+                groups.push_back(g);
+                group_items.emplace_back();
+                gidx = (int)groups.size() - 1;
+            }
+            groups[gidx].N = std::max(groups[gidx].N, W);
+            groups[gidx].hp = std::max(groups[gidx].hp, p->umma_hp);
+        }
         const int16_t kind = W == 1 ? (int16_t)U_SPMV : spmm_kind(nt, terms);
         const int32_t cls = W == 1 ? 2 : (terms ? 0 : 1);
         const int64_t nsplit = std::max<int32_t>(p->n_split_tiles, 1);
@@ -416,9 +488,15 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
             r.off += rec_base;
             const int32_t idx = (int32_t)items.size();
             items.push_back(r);
-            item_tcoff.push_back(terms && !p->tcoff_host.empty() ? tc_base + p->tcoff_host[k] : -1);
+            item_tcoff.push_back(terms && !umma && !p->tcoff_host.empty() ? tc_base + p->tcoff_host[k] : -1);
             item_mat.push_back(i);
             if (kind == U_SPMV) bt->stage_bytes = std::max(bt->stage_bytes, r.bytes);
+            if (umma) {
+                const int64_t po = p->umma_off_host[k];
+                group_items[gidx].push_back({r, po >= 0 ? umma_base + po : -1});
+                bt->n_units += slices;
+                continue;
+            }
             for (int sl = 0; sl < slices; ++sl) {
                 Sortable s;
                 s.cls = cls;
@@ -435,8 +513,11 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
                 splits.push_back(t);
             }
         rec_base += p->records_bytes;
-        if (terms && !p->tcoff_host.empty()) tc_base += p->tc_words;
+        if (terms && !umma && !p->tcoff_host.empty()) tc_base += p->tc_words;
+        if (umma) umma_base += p->umma_bytes;
     }
+    for (auto &gi : group_items)   // largest first
+        std::stable_sort(gi.begin(), gi.end(), [](const UmmaItem &a, const UmmaItem &b) { return a.r.bytes > b.r.bytes; });
     std::stable_sort(q.begin(), q.end(), [](const Sortable &a, const Sortable &b) {
         return a.cls != b.cls ? a.cls < b.cls : a.cost > b.cost;
     });
@@ -446,8 +527,9 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
         units[k] = q[k].u;
         spmm_smem = std::max(spmm_smem, spmm_unit_smem(q[k].u.kind, item_tcoff[q[k].u.item] >= 0));
     }
-    bt->n_units = (int64_t)units.size();
-    if (bt->n_units >= INT32_MAX) return bail(fail(SABLE_ERR_UNSUPPORTED, "batch of %lld units", (long long)bt->n_units));
+    bt->n_queue = (int64_t)units.size();
+    bt->n_units += bt->n_queue;
+    if (bt->n_queue >= INT32_MAX) return bail(fail(SABLE_ERR_UNSUPPORTED, "batch of %lld units", (long long)bt->n_queue));
     bt->stage_bytes = (bt->stage_bytes + 127) & ~127;
     bool has_spmm = false;
     for (const BatchUnit &u : units) has_spmm |= u.kind != U_SPMV;
@@ -493,6 +575,17 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
         if ((rc = dev_alloc(&bt->d_tcoff, item_tcoff.size(), &bytes, "split-BF16 offsets"))) return bail(rc);
     }
     if ((rc = dev_alloc(&bt->d_items, items.size(), &bytes, "items"))) return bail(rc);
+    if (umma_base > 0 && (rc = dev_alloc(&bt->d_umma, (size_t)umma_base, &bytes, "tcgen05 panel terms"))) return bail(rc);
+    for (size_t g = 0; g < groups.size(); ++g) {
+        UmmaGroup &G = groups[g];
+        G.n_items = (int)group_items[g].size();
+        if ((rc = dev_alloc(&G.d_items, group_items[g].size(), &bytes, "tcgen05 items"))) return bail(rc);
+        if ((rc = dev_alloc(&G.d_off, group_items[g].size(), &bytes, "tcgen05 term offsets"))) {
+            bt->umma.push_back(G);
+            return bail(rc);
+        }
+        bt->umma.push_back(G);
+    }
     if ((rc = dev_alloc(&bt->d_units, units.size(), &bytes, "units"))) return bail(rc);
     if ((rc = dev_alloc(&bt->d_mats, mats.size(), &bytes, "matrix table"))) return bail(rc);
     if ((rc = dev_alloc(&bt->d_partial, (size_t)partial_total, &bytes, "partials"))) return bail(rc);
@@ -516,13 +609,32 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
         int64_t wb = 0;
         for (int i = 0; i < n_plans && e == cudaSuccess; ++i) {
             const sable_plan *p = plans[i];
-            const bool tc = widths[i] >= 32 && p->spmm_tc && !p->tcoff_host.empty();
+            const bool tc = widths[i] >= 32 && p->spmm_tc && !p->tcoff_host.empty() && !runs_umma(p, widths[i]);
             if (!tc) continue;
             e = cudaMemcpy(bt->d_tcplanes + wb, p->d_tcplanes, (size_t)p->tc_words * sizeof(uint4), cudaMemcpyDeviceToDevice);
             wb += p->tc_words;
         }
         if (e == cudaSuccess)
             e = cudaMemcpy(bt->d_tcoff, item_tcoff.data(), item_tcoff.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    }
+    if (umma_base > 0) {
+        int64_t ub = 0;
+        for (int i = 0; i < n_plans && e == cudaSuccess; ++i) {
+            const sable_plan *p = plans[i];
+            if (!runs_umma(p, widths[i])) continue;
+            e = cudaMemcpy(bt->d_umma + ub, p->d_umma, (size_t)p->umma_bytes, cudaMemcpyDeviceToDevice);
+            ub += p->umma_bytes;
+        }
+    }
+    for (size_t g = 0; g < bt->umma.size() && e == cudaSuccess; ++g) {
+        std::vector<ItemRef> gr;
+        std::vector<int64_t> go;
+        for (const UmmaItem &it : group_items[g]) {
+            gr.push_back(it.r);
+            go.push_back(it.off);
+        }
+        e = cudaMemcpy(bt->umma[g].d_items, gr.data(), gr.size() * sizeof(ItemRef), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(bt->umma[g].d_off, go.data(), go.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_items, items.data(), items.size() * sizeof(ItemRef), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -559,7 +671,7 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     if (e != cudaSuccess) return bail(cuda_fail(e, "batch kernel occupancy"));
     occ = std::max(occ, 1);
     const int per_sm = o.ctas_per_sm ? std::min(o.ctas_per_sm, occ) : occ;
-    bt->n_ctas = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, std::max<int64_t>(bt->n_units, 1)));
+    bt->n_ctas = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, std::max<int64_t>(bt->n_queue, 1)));
     e = cudaEventCreateWithFlags(&bt->done, cudaEventDisableTiming);
     if (e != cudaSuccess) return bail(cuda_fail(e, "batch event"));
     if (bt->use_graph) {

@@ -31,8 +31,12 @@ spmm_umma_kernel(const LaunchArgs la, const int64_t part_stride, const int bst, 
     const int item = blockIdx.x, slice = blockIdx.y;
     const unsigned char *R = la.records + la.items[item].off;
     const MatIO &a = mat_of(la, reinterpret_cast<const ItemHeader *>(R)->mat);
+    // a batch launches as many N-slices as its widest matrix needs; the CTAs
+    // of a narrower matrix's missing slices leave (uniformly, before any barrier)
+    if (slice * NT >= a.N) return;
     const int64_t po = la.umma_off[item];
-    spmm_umma_item<NT, TERMS>(R, a, slice, part_stride, smem, la.umma + (po > 0 ? po : 0), la.error, bst, bstage);
+    spmm_umma_item<NT, TERMS>(R, a, slice, la.mats ? a.part_stride : part_stride, smem, la.umma + (po > 0 ? po : 0),
+                              la.error, bst, bstage);
     if (TIMED) {
         __syncthreads();
         if (threadIdx.x == 0) la.cycles[(int64_t)slice * la.n_items + item] = (int64_t)(clock64() - t0);

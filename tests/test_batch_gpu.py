@@ -165,3 +165,43 @@ def test_batch_256_generator_distribution(cuda):
         assert r["pass"], (k, w, r)
         worst = max(worst, r["max"])
     assert worst <= oracle.TOL
+
+
+def test_batch_tcgen05_spmm_bitwise_equals_single_plan(cuda):
+    """Split-BF16 SpMM matrices whose plans hold tcgen05 panel terms run on the
+    tcgen05 kernel inside the batch (one launch per N-slice width, widths 32
+    to 256, a 96-wide matrix sharing the 128-wide group's launch): identical
+    bits to each plan's own sable_spmm, next to a plan on the mma.sync kernel
+    (in the persistent kernel's queue) and SpMV matrices, all within the
+    tolerance of FP64."""
+    import torch
+    cases = [(900, 64, "split3", "umma", 4096), (700, 32, "split3", "umma", 0), (600, 96, "split3", "umma", 0),
+             (500, 128, "split3", "umma", 8192), (400, 256, "split3", "umma", 0), (800, 64, "split2", "umma", 0),
+             (650, 64, "split3", "mma_sync", 0), (1500, 1, False, "umma", 0), (300, 8, False, "umma", 0)]
+    mats, plans, xs = [], [], []
+    for k, (n, w, tc, kern, cb) in enumerate(cases):
+        m = random_vbr(500 + k, n)
+        dense = np.random.default_rng(600 + k).random(m.n_blocks) < 0.7
+        comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense)
+        mats.append((m, comp))
+        plans.append(Plan(comp, spmm_tc=tc, chunk_bytes=cb, tc_kernel=kern,
+                          split_layout="mixed" if w == 1 else "separate"))
+        rng = np.random.default_rng(700 + k)
+        xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
+    widths = [c[1] for c in cases]
+    for use_graph in (False, True):
+        b = Batch(plans, widths, use_graph=use_graph)
+        ys = b.outputs()
+        b.run(xs, ys)
+        b.run(xs, ys)
+        b.check()
+        torch.cuda.synchronize()
+        for k, ((m, comp), p, x, y, c) in enumerate(zip(mats, plans, xs, ys, cases)):
+            w, tc, kern = c[1], c[2], c[3]
+            xn = x.cpu().numpy()
+            yr, ya = oracle.spmv_vbrc(comp, xn) if w == 1 else oracle.spmm_vbr(m, xn)
+            r = oracle.report(y.cpu().numpy(), yr, ya, oracle.TOL_SPLIT2 if tc == "split2" else oracle.TOL)
+            assert r["pass"], (k, c, r)
+            if w >= 32 and kern == "umma":
+                assert torch.equal(p.spmm(x), y), (k, c)
+        b.close()
