@@ -270,7 +270,7 @@ def bench_batch(reps: int, cpu: bool = True) -> dict:
         xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
         ys.append(torch.empty(m.n_rows if w == 1 else (m.n_rows, w), device="cuda"))
     from oracle import oracle
-    plain, learned, learned_comps = [], [], []
+    plain, learned_comps = [], []
     errs_med = []
     nnz_work = 0
     for m, w in zip(mats, widths):
@@ -282,7 +282,6 @@ def bench_batch(reps: int, cpu: bool = True) -> dict:
                           split_layout=lay))
         learned_comps.append(convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mlp,
                                               bt=bt))
-        learned.append(Plan(learned_comps[-1], spmm_tc="split3", split_layout=lay))
 
     def run_plain():
         for p, x, y, w in zip(plain, xs, ys, widths):
@@ -292,7 +291,8 @@ def bench_batch(reps: int, cpu: bool = True) -> dict:
                 p.spmm(x, y)
 
     ms_p = autotune.time_ms(run_plain, reps)
-    batch, table = autotune.tune_batch(learned, widths, xs, ys)
+    # the batch autotuner builds the learned plans per shape from the same choices
+    batch, table = autotune.tune_batch(learned_comps, widths, xs, ys, spmm_tc="split3")
     ms_b = autotune.time_ms(lambda: batch.run(xs, ys), reps)
     info = batch.info()
     # every one of the batch's outputs against the FP64 oracle
@@ -305,7 +305,7 @@ def bench_batch(reps: int, cpu: bool = True) -> dict:
         r = oracle.report(y.cpu().numpy(), yr, ya)
         errs.append(r["max"])
         errs_med.append(r["median"])
-    for p in plain + learned:
+    for p in plain:
         p.close()
     batch.close()
     cpu_b = None

@@ -163,24 +163,85 @@ def tune(comp: Compressed, x, y, N: int = 1, spmm_tc="split3", candidates=None, 
     return best
 
 
-def tune_batch(plans, widths, xs, ys, stages=(2, 4), reps: int = 10) -> tuple[Batch, list]:
-    """Pick the ring depth of a batch (CUDA graph on); returns (batch, table)."""
-    table, best, best_ms = [], None, float("inf")
-    for s in stages:
+# Batch shapes per matrix class: the SpMV matrices' executor (per-warp kernel
+# on compact records, or the batch's ring of per-CTA items) and the SpMM
+# matrices' work-item size (whole block rows for the tcgen05 kernel, or
+# smaller items); the ring depth only matters when ring units remain.
+BATCH_SPMV_SHAPES = [
+    {"executor": "warp_items", "row_tile": 16, "chunk_bytes": 32768},
+    {"executor": "warp_items", "row_tile": 16, "chunk_bytes": 16384},
+    {"executor": "ring", "row_tile": 128, "chunk_bytes": 32768},
+]
+BATCH_SPMM_SHAPES = [
+    {"executor": "items", "row_tile": 128, "chunk_bytes": 262144},
+    {"executor": "items", "row_tile": 128, "chunk_bytes": 131072},
+    {"executor": "items", "row_tile": 128, "chunk_bytes": 32768},
+]
+
+
+def _batch_plan(comp: Compressed, shape: dict, N: int, spmm_tc) -> Plan:
+    return Plan(comp, row_tile=shape["row_tile"], chunk_bytes=shape["chunk_bytes"],
+                spmm_tc=spmm_tc if N > 1 else "off", split_layout="mixed" if N == 1 else "separate",
+                schedule="warp_items" if shape["executor"] == "warp_items" else "items")
+
+
+def tune_batch(comps, widths, xs, ys, spmm_tc="split3", stages=(2, 4), reps: int = 10) -> tuple[Batch, list]:
+    """Pick a batch's shape by timing it whole (CUDA graph on): the SpMV
+    matrices' executor and item shape, then the SpMM matrices' item size,
+    then the ring depth when ring units remain (one class at a time, the
+    others held at their best so far).  Returns (batch, table); the batch
+    owns copies of the records, its plans are closed."""
+    widths = [int(w) for w in widths]
+    spmv = [i for i, w in enumerate(widths) if w == 1]
+    spmm = [i for i, w in enumerate(widths) if w > 1]
+    plan_cache: dict = {}
+
+    def plans_for(idx, shape):
+        key = (tuple(idx), tuple(sorted(shape.items())))
+        if key not in plan_cache:
+            plan_cache[key] = [_batch_plan(comps[i], shape, widths[i], spmm_tc) for i in idx]
+        return plan_cache[key]
+
+    table, best, best_ms, best_cfg = [], None, float("inf"), None
+
+    def trial(sv, sm, st):
+        nonlocal best, best_ms, best_cfg
+        cfg = {"spmv": sv, "spmm": sm, "stages": st}
+        plans = [None] * len(widths)
+        if spmv:
+            for i, p in zip(spmv, plans_for(spmv, sv)):
+                plans[i] = p
+        if spmm:
+            for i, p in zip(spmm, plans_for(spmm, sm)):
+                plans[i] = p
         try:
-            b = Batch(plans, widths, use_graph=True, stages=s)
+            b = Batch(plans, widths, use_graph=True, stages=st)
         except Exception as ex:
-            table.append({"stages": s, "ms": None, "error": str(ex)[:80]})
-            continue
+            table.append({**cfg, "ms": None, "error": str(ex)[:80]})
+            return
         ms = time_ms(lambda: b.run(xs, ys), reps)
         b.check()
-        table.append({"stages": s, "ms": round(ms, 5), "n_ctas": b.info()["n_ctas"]})
+        table.append({**cfg, "ms": round(ms, 5), "n_ctas": b.info()["n_ctas"]})
         if ms < best_ms:
             if best is not None:
                 best.close()
-            best, best_ms = b, ms
+            best, best_ms, best_cfg = b, ms, cfg
         else:
             b.close()
+
+    sv0, sm0 = BATCH_SPMV_SHAPES[0], BATCH_SPMM_SHAPES[0]
+    for sv in (BATCH_SPMV_SHAPES if spmv else [sv0]):
+        trial(sv, sm0, 0)
+    sv_best = best_cfg["spmv"] if best_cfg else sv0
+    for sm in (BATCH_SPMM_SHAPES[1:] if spmm else []):
+        trial(sv_best, sm, 0)
+    if best_cfg is not None and best.info()["n_units"] > 0 and (best_cfg["spmv"]["executor"] == "ring" or any(
+            widths[i] < 32 for i in spmm)):
+        for st in stages:
+            trial(best_cfg["spmv"], best_cfg["spmm"], st)
+    for ps in plan_cache.values():
+        for p in ps:
+            p.close()
     if best is None:
         raise RuntimeError("no batch shape could be built")
     return best, table

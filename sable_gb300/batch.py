@@ -5,8 +5,12 @@
 
 width 1 runs SpMV on that matrix, width N > 1 (a multiple of 4) SpMM of
 width N.  The batch copies the plans' device records at creation, so the
-plans may be closed afterwards.  One kernel launch (or one CUDA graph
-launch) per run, whatever the number of matrices.
+plans may be closed afterwards.  One CUDA graph launch per run (or, without
+the graph, the same launches in a row), whatever the number of matrices:
+the tcgen05 kernel over the split-BF16 SpMM matrices (one launch per N-slice
+width), the per-warp kernel over the SpMV matrices of per-warp plans, the
+persistent kernel over the work queue of the rest, and the combine of split
+tiles, each only when it has work.
 """
 from __future__ import annotations
 

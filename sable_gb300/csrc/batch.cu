@@ -17,6 +17,10 @@
 // tcgen05 kernel (spmm_umma.cu), one launch per N-slice width over the items
 // of all such matrices (largest first, each CTA reading its matrix from the
 // batch's matrix table), before the persistent kernel, in the same graph.
+// Likewise the SpMV matrices of plans of the per-warp executor (compact
+// records) run on the per-warp kernel (spmv.cu), one launch over all their
+// items, largest first, with a per-item matrix table; those records combine
+// their split tiles themselves.
 // The other SpMM units run the bodies of spmm_item.cuh from global memory.  SpMV units
 // run the CTA-per-item body (spmv_item.cuh) from an S-stage TMA ring that
 // keeps S claimed records in flight per CTA (S = 2..8; by default the
@@ -263,6 +267,9 @@ struct UmmaGroup {
 struct sable_batch {
     int device = 0;
     std::vector<UmmaGroup> umma;
+    int n_warp_items = 0;                // per-warp SpMV items (compact records)
+    ItemRef *d_warp_items = nullptr;     // their merged records, largest first
+    int32_t *d_warp_mat = nullptr;       // and their matrices
     unsigned char *d_umma = nullptr;     // merged tcgen05 panel terms
     int n_mats = 0;
     std::vector<int32_t> width;
@@ -321,6 +328,18 @@ int batch_launch(sable_batch *bt, cudaStream_t s) {
         const int ec = launch_spmm_umma(la, g.N, g.nt, g.terms, 0, false, s);
         if (ec) return cuda_fail((cudaError_t)ec, "batch tcgen05 SpMM launch");
     }
+    if (bt->n_warp_items > 0) {
+        LaunchArgs la;
+        memset(&la, 0, sizeof la);
+        la.records = bt->d_records;
+        la.items = bt->d_warp_items;
+        la.item_mat = bt->d_warp_mat;
+        la.mats = bt->d_mats;
+        la.error = bt->d_error;
+        la.n_items = bt->n_warp_items;
+        const int ec = launch_spmv_warp_items(la, false, s);
+        if (ec) return cuda_fail((cudaError_t)ec, "batch per-warp SpMV launch");
+    }
     cudaError_t e = cudaSuccess;
     if (bt->n_queue > 0) {
         e = cudaMemsetAsync(bt->d_head, 0, sizeof(int), s);
@@ -375,6 +394,8 @@ int sable_batch_destroy(sable_batch *bt) {
         cudaFree(g.d_off);
     }
     cudaFree(bt->d_umma);
+    cudaFree(bt->d_warp_items);
+    cudaFree(bt->d_warp_mat);
     if (bt->h_mats) cudaFreeHost(bt->h_mats);
     if (prev >= 0) cudaSetDevice(prev);
     delete bt;
@@ -391,9 +412,11 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     for (int i = 0; i < n_plans; ++i) {
         if (!plans[i]) return fail(SABLE_ERR_ARG, "plan %d is null", i);
         if (plans[i]->device != plans[0]->device) return fail(SABLE_ERR_ARG, "plans on different devices");
-        if (plans[i]->compact)
-            return fail(SABLE_ERR_UNSUPPORTED, "plan %d: a plan of the per-warp SpMV executor (schedule 2) is not batched", i);
-        if (!plans[i]->staged_ok)
+        if (plans[i]->compact && widths[i] != 1)
+            return fail(SABLE_ERR_UNSUPPORTED, "plan %d: a plan of the per-warp SpMV executor (schedule 2) runs SpMV only", i);
+        // the tcgen05 and per-warp kernels stream their records; everything
+        // else in a batch stages whole records in shared memory
+        if (!plans[i]->staged_ok && !runs_umma(plans[i], widths[i]) && !plans[i]->compact)
             return fail(SABLE_ERR_UNSUPPORTED, "plan %d: work items larger than the batch's staging (%d bytes)", i,
                         SABLE_MAX_ITEM_BYTES);
         if (widths[i] < 1 || (widths[i] > 1 && (widths[i] & 3)))
@@ -441,6 +464,11 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     };
     std::vector<UmmaGroup> groups;
     std::vector<std::vector<UmmaItem>> group_items;
+    struct WarpItem {
+        ItemRef r;
+        int32_t mat;
+    };
+    std::vector<WarpItem> warp_items;
     int64_t umma_base = 0;
     for (int i = 0; i < n_plans; ++i) {
         const sable_plan *p = plans[i];
@@ -486,6 +514,11 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
         for (int64_t k = 0; k < p->n_items; ++k) {
             ItemRef r = p->items_host[k];
             r.off += rec_base;
+            if (p->compact) {   // the per-warp kernel; its header layout has no matrix field
+                warp_items.push_back({r, i});
+                bt->n_units += 1;
+                continue;
+            }
             const int32_t idx = (int32_t)items.size();
             items.push_back(r);
             item_tcoff.push_back(terms && !umma && !p->tcoff_host.empty() ? tc_base + p->tcoff_host[k] : -1);
@@ -507,7 +540,7 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
                 q.push_back(s);
             }
         }
-        if (W == 1)
+        if (W == 1 && !p->compact)   // compact records combine their split tiles themselves
             for (SplitTile t : p->splits_host) {
                 t.mat = i;
                 splits.push_back(t);
@@ -516,6 +549,8 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
         if (terms && !umma && !p->tcoff_host.empty()) tc_base += p->tc_words;
         if (umma) umma_base += p->umma_bytes;
     }
+    std::stable_sort(warp_items.begin(), warp_items.end(),
+                     [](const WarpItem &a, const WarpItem &b) { return a.r.cost > b.r.cost; });
     for (auto &gi : group_items)   // largest first
         std::stable_sort(gi.begin(), gi.end(), [](const UmmaItem &a, const UmmaItem &b) { return a.r.bytes > b.r.bytes; });
     std::stable_sort(q.begin(), q.end(), [](const Sortable &a, const Sortable &b) {
@@ -576,6 +611,11 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
     }
     if ((rc = dev_alloc(&bt->d_items, items.size(), &bytes, "items"))) return bail(rc);
     if (umma_base > 0 && (rc = dev_alloc(&bt->d_umma, (size_t)umma_base, &bytes, "tcgen05 panel terms"))) return bail(rc);
+    bt->n_warp_items = (int)warp_items.size();
+    if (!warp_items.empty()) {
+        if ((rc = dev_alloc(&bt->d_warp_items, warp_items.size(), &bytes, "per-warp items"))) return bail(rc);
+        if ((rc = dev_alloc(&bt->d_warp_mat, warp_items.size(), &bytes, "per-warp item matrices"))) return bail(rc);
+    }
     for (size_t g = 0; g < groups.size(); ++g) {
         UmmaGroup &G = groups[g];
         G.n_items = (int)group_items[g].size();
@@ -635,6 +675,16 @@ int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t 
         }
         e = cudaMemcpy(bt->umma[g].d_items, gr.data(), gr.size() * sizeof(ItemRef), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(bt->umma[g].d_off, go.data(), go.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess && !warp_items.empty()) {
+        std::vector<ItemRef> wr;
+        std::vector<int32_t> wm;
+        for (const WarpItem &w : warp_items) {
+            wr.push_back(w.r);
+            wm.push_back(w.mat);
+        }
+        e = cudaMemcpy(bt->d_warp_items, wr.data(), wr.size() * sizeof(ItemRef), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(bt->d_warp_mat, wm.data(), wm.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) e = cudaMemcpy(bt->d_items, items.data(), items.size() * sizeof(ItemRef), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)

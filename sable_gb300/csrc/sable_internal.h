@@ -158,6 +158,7 @@ struct LaunchArgs {
     const WorkRef *work;    // persistent: worker lists, concatenated
     const int *cta_begin;   // persistent: worker w's entries are [cta_begin[w], cta_begin[w+1])
     const MatIO *mats;      // per matrix (batch); nullptr: every item uses mat0
+    const int32_t *item_mat;  // per-warp SpMV of a batch: matrix of each item (compact headers carry none)
     MatIO mat0;
     int64_t *cycles;        // per-item SM cycles (timed variant) or nullptr
     const void *tcplanes;   // SpMM split-BF16: pre-split A fragments (uint4 words) or nullptr

@@ -261,9 +261,9 @@ __device__ __forceinline__ void warp_csr_window(const float *val, const uint16_t
 // split tile, to the item's partial rows, the last of the tile's items adding
 // them into y.  rows: SABLE_CW_MAX_ROWS floats, xw: WI_XW floats of the
 // warp's shared memory.  TIMED: SM cycles of the item into a.cycles[item].
-template <bool TIMED>
+template <bool TIMED, bool BATCH>
 __device__ __forceinline__ void warp_item(const LaunchArgs &a, int item, int64_t off, int bytes, int lane, float *rows,
-                                          float *xw) {
+                                          float *xw, int mat) {
     long long t0 = 0;
     if (TIMED && lane == 0) t0 = clock64();
     const unsigned char *R = a.records + off;
@@ -272,7 +272,7 @@ __device__ __forceinline__ void warp_item(const LaunchArgs &a, int item, int64_t
         if (lane == 0) atomicExch(a.error, 1);
         return;
     }
-    const MatIO &io = a.mat0;
+    const MatIO &io = BATCH ? a.mats[mat] : a.mat0;
     const int h = hd.h, nq = hd.nq, ns = hd.ns;
     __syncwarp();  // the previous item's reads of rows / xw are done
     for (int i = lane; i < h; i += 32) rows[i] = 0.f;
@@ -369,8 +369,10 @@ __device__ __forceinline__ void warp_item(const LaunchArgs &a, int item, int64_t
     }
 }
 
-// One compact item per warp, in item-table order (largest first).
-template <bool TIMED>
+// One compact item per warp, in item-table order (largest first); BATCH:
+// items of many matrices (a.item_mat, a.mats), a form of its own so that the
+// one-matrix kernel keeps its registers.
+template <bool TIMED, bool BATCH>
 __global__ void __launch_bounds__(WI_WARPS * 32, 32 / WI_WARPS)
 spmv_warp_items_kernel(const LaunchArgs a) {
     __shared__ float s_rows[WI_WARPS][SABLE_CW_MAX_ROWS];  // CSR row sums of each warp's item
@@ -379,8 +381,9 @@ spmv_warp_items_kernel(const LaunchArgs a) {
     const int item = blockIdx.x * WI_WARPS + w;
     if (item >= a.n_items) return;  // the whole warp leaves; no CTA barrier follows
     const ItemRef ref = a.items[item];
+    const int mat = BATCH ? a.item_mat[item] : 0;   // a batch's matrix (loaded beside the item)
     if (lane == 0) prefetch_record(a.records + ref.off, ref.bytes);
-    warp_item<TIMED>(a, item, ref.off, ref.bytes, lane, s_rows[w], s_xw[w]);
+    warp_item<TIMED, BATCH>(a, item, ref.off, ref.bytes, lane, s_rows[w], s_xw[w], mat);
 }
 
 // dst[0, n) = src[0, n) (either side may be mapped host memory): 16-byte
@@ -668,8 +671,9 @@ int launch_spmv_warp_items(const LaunchArgs &a, bool timed, void *stream) {
     if (a.n_items <= 0) return 0;
     const unsigned grid = (a.n_items + WI_WARPS - 1) / WI_WARPS;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if (timed) spmv_warp_items_kernel<true><<<grid, WI_WARPS * 32, 0, s>>>(a);
-    else spmv_warp_items_kernel<false><<<grid, WI_WARPS * 32, 0, s>>>(a);
+    if (a.item_mat && a.mats) spmv_warp_items_kernel<false, true><<<grid, WI_WARPS * 32, 0, s>>>(a);
+    else if (timed) spmv_warp_items_kernel<true, false><<<grid, WI_WARPS * 32, 0, s>>>(a);
+    else spmv_warp_items_kernel<false, false><<<grid, WI_WARPS * 32, 0, s>>>(a);
     return (int)cudaGetLastError();
 }
 

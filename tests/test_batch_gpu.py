@@ -138,8 +138,9 @@ def test_batch_256_generator_distribution(cuda):
     """40 matrices from the 256-matrix batch workload's generator (rows
     log-uniform in [1000, 20000], partitions U[4,128], block p = 0.02, SpMM
     width 64 for every second matrix), each with the learned block choice at
-    its width, SpMM units in split BF16 (three terms), all in one CUDA-graph
-    launch; every output against the FP64 oracle."""
+    its width, SpMM matrices in split BF16 (three terms) on the tcgen05 kernel
+    with whole block rows per item, all in one CUDA-graph launch; every
+    output against the FP64 oracle."""
     import torch
     from sable_gb300 import blockmodel
     mats, widths = synth.batch_256(count=40)
@@ -151,7 +152,8 @@ def test_batch_256_generator_distribution(cuda):
         dense = model.choose_dense(convert.block_features(m.val, bt, w))
         comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense, bt=bt)
         comps.append(comp)
-        plans.append(Plan(comp, spmm_tc="split3", split_layout="mixed" if w == 1 else "separate"))
+        shape = {} if w == 1 else {"row_tile": 128, "chunk_bytes": 262144}   # whole block rows (tcgen05)
+        plans.append(Plan(comp, spmm_tc="split3", split_layout="mixed" if w == 1 else "separate", **shape))
         xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
     b = Batch(plans, widths, use_graph=True)
     ys = b.outputs()
@@ -205,3 +207,67 @@ def test_batch_tcgen05_spmm_bitwise_equals_single_plan(cuda):
             if w >= 32 and kern == "umma":
                 assert torch.equal(p.spmm(x), y), (k, c)
         b.close()
+
+
+def test_batch_per_warp_spmv_plans(cuda):
+    """SpMV matrices whose plans hold compact records (the per-warp executor)
+    run on the per-warp kernel inside the batch, with a per-item matrix
+    table and split tiles combined in the kernel: identical bits to each
+    plan's own sable_spmv, next to SpMV matrices on the batch's ring and SpMM
+    matrices on the tcgen05 kernel; with and without a graph, twice."""
+    import torch
+    cases = [(3000, 1, "warp_items", 16, 8192), (1200, 1, "warp_items", 8, 4096), (5000, 1, "warp_items", 32, 32768),
+             (200, 1, "warp_items", 64, 4096), (2000, 1, "items", 128, 4096), (900, 64, "items", 128, 0),
+             (4000, 1, "warp_items", 16, 32768)]
+    mats, plans, xs = [], [], []
+    for k, (n, w, sched, rt, cb) in enumerate(cases):
+        m = random_vbr(800 + k, n)
+        dense = np.random.default_rng(900 + k).random(m.n_blocks) < 0.5
+        comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense)
+        mats.append((m, comp))
+        plans.append(Plan(comp, schedule=sched, row_tile=rt, chunk_bytes=cb, spmm_tc="split3" if w > 1 else False))
+        rng = np.random.default_rng(1000 + k)
+        xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
+    assert any(p.stats()["scratch_floats"] > 0 for p, c in zip(plans, cases) if c[2] == "warp_items")
+    widths = [c[1] for c in cases]
+    for use_graph in (False, True):
+        b = Batch(plans, widths, use_graph=use_graph)
+        ys = b.outputs()
+        for _ in range(2):
+            b.run(xs, ys)
+        b.check()
+        torch.cuda.synchronize()
+        for k, ((m, comp), p, x, y, c) in enumerate(zip(mats, plans, xs, ys, cases)):
+            xn = x.cpu().numpy()
+            yr, ya = oracle.spmv_vbrc(comp, xn) if c[1] == 1 else oracle.spmm_vbr(m, xn)
+            r = oracle.report(y.cpu().numpy(), yr, ya)
+            assert r["pass"], (k, c, r)
+            if c[1] == 1:
+                assert torch.equal(p.spmv(x), y), (k, c)
+        b.close()
+
+
+def test_tune_batch_picks_a_shape_per_class(cuda):
+    """The batch autotuner times whole batches over the SpMV executors and
+    item shapes and the SpMM item sizes; the batch it returns gives the FP64
+    oracle's results."""
+    import torch
+    from sable_gb300 import autotune
+    mats, widths = synth.batch_256(count=12)
+    rng = np.random.default_rng(12)
+    comps, xs, ys = [], [], []
+    for m, w in zip(mats, widths):
+        dense = rng.random(m.n_blocks) < 0.6
+        comps.append(convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, dense))
+        xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
+        ys.append(torch.empty(m.n_rows if w == 1 else (m.n_rows, w), device="cuda"))
+    b, table = autotune.tune_batch(comps, widths, xs, ys, reps=3)
+    assert len([t for t in table if t["ms"] is not None]) >= len(autotune.BATCH_SPMV_SHAPES)
+    b.run(xs, ys)
+    b.check()
+    for m, comp, w, x, y in zip(mats, comps, widths, xs, ys):
+        xn = x.cpu().numpy()
+        yr, ya = oracle.spmv_vbrc(comp, xn) if w == 1 else oracle.spmm_vbr(m, xn)
+        r = oracle.report(y.cpu().numpy(), yr, ya)
+        assert r["pass"], (w, r)
+    b.close()

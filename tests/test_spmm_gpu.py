@@ -92,7 +92,9 @@ def test_spmm_host_entry(cuda):
 def test_large_items_spmm_only(cuda, N, tc):
     """Work items above the shared-memory staging size (256 KB: whole block
     rows per item, long K loops, no split tiles): SpMM parity, and SpMV and
-    batching refuse the plan instead of staging records that do not fit."""
+    the batch's staged executors refuse the plan instead of staging records
+    that do not fit; a batch takes it when its matrix runs on the tcgen05
+    kernel (split BF16, which streams records), with the plan's own bits."""
     import torch
     from sable_gb300 import _lib
     from sable_gb300.batch import Batch
@@ -109,6 +111,17 @@ def test_large_items_spmm_only(cuda, N, tc):
     assert r["pass"], r
     with pytest.raises(_lib.SableError, match="SpMM-only"):
         plan.spmv(torch.zeros(m.n_cols, device="cuda"))
+    if tc:
+        b = Batch([plan], [N])
+        Xd = torch.as_tensor(X).cuda()
+        Yb = torch.empty(m.n_rows, N, device="cuda")
+        b.run([Xd], [Yb])
+        b.check()
+        np.testing.assert_array_equal(Yb.cpu().numpy(), Y)
+        b.close()
+    else:
+        with pytest.raises(_lib.SableError, match="staging"):
+            Batch([plan], [N])
     with pytest.raises(_lib.SableError, match="staging"):
-        Batch([plan], [N])
+        Batch([plan], [1])
     plan.close()

@@ -157,8 +157,9 @@ def test_compact_csr_row_lengths(cuda, row_tile, chunk_bytes, dense_frac):
 
 
 def test_compact_plan_is_spmv_only(cuda):
-    """A plan of the per-warp executor holds compact records: SpMM and
-    batching refuse it with SABLE_ERR_UNSUPPORTED instead of misreading them."""
+    """A plan of the per-warp executor holds compact records: SpMM, and a
+    batch asked for a width above 1, refuse it with SABLE_ERR_UNSUPPORTED
+    instead of misreading them."""
     import torch
     from sable_gb300 import _lib
     from sable_gb300.batch import Batch
@@ -168,8 +169,8 @@ def test_compact_plan_is_spmv_only(cuda):
     X = torch.zeros(m.n_cols, 8, device="cuda")
     with pytest.raises(_lib.SableError, match="SpMV only"):
         plan.spmm(X)
-    with pytest.raises(_lib.SableError, match="not batched"):
-        Batch([plan], [1])
+    with pytest.raises(_lib.SableError, match="SpMV only"):
+        Batch([plan], [4])
 
 
 def test_deterministic_and_host_entry(cuda):
