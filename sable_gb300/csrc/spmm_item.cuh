@@ -374,15 +374,78 @@ __device__ __forceinline__ void spmm_tile_finish(const unsigned char *R, const I
             s_wrow[lane] = lane == 8 ? h : lo;
         }
         __syncthreads();
+        // A row's entries go 32 at a time: one coalesced load (an entry per
+        // lane), then each row subgroup rs takes entries rs, rs + RSUB, ... of
+        // the chunk by shuffle, CSR_U X rows in flight per lane, so no X load
+        // waits for its entry's load.  Each lane adds its entries in
+        // increasing order, as one entry at a time would.
+        constexpr int CSR_U = 4;
+        if constexpr (RSUB == 1) {
+            // NT = 128: the 32 lanes are the 32 column quads, so a warp streams
+            // the entries of all its rows as one sequence (rows are contiguous)
+            // and adds a row's sum into the Y tile when the sequence leaves it:
+            // the X loads of consecutive rows overlap instead of each row
+            // paying its own load latencies.
+            const int r_lo = act ? s_wrow[warp] : 0, r_hi = act ? s_wrow[warp + 1] : 0;
+            if (r_lo < r_hi) {
+                const int e_lo = rst[r_lo], e_hi = rst[r_hi];
+                int r = r_lo, r_end = rst[r_lo + 1];
+                float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int c0 = e_lo; c0 < e_hi; c0 += 32) {
+                    const int cnt = min(32, e_hi - c0);
+                    const uint2 mine = lane < cnt ? __ldg(E + c0 + lane) : make_uint2(0u, 0u);
+                    for (int k0 = 0; k0 < cnt; k0 += CSR_U) {
+                        float4 xv[CSR_U];
+                        float vv[CSR_U];
+#pragma unroll
+                        for (int u = 0; u < CSR_U; ++u) {
+                            const int k = k0 + u;
+                            const int src = k < 32 ? k : 31;
+                            vv[u] = __uint_as_float(__shfl_sync(FULL, mine.x, src));
+                            const uint32_t col = __shfl_sync(FULL, mine.y, src);
+                            xv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (k < cnt && col_ok)
+                                xv[u] = __ldg(reinterpret_cast<const float4 *>(X + (int64_t)col * a.ldx + n0 + 4 * cq));
+                        }
+#pragma unroll
+                        for (int u = 0; u < CSR_U; ++u) {
+                            const int k = k0 + u;
+                            if (k >= cnt) break;
+                            while (c0 + k >= r_end) {   // row r is complete (warp-uniform)
+                                if (r_end > rst[r]) ys4[r * CQ + cq] = add4(ys4[r * CQ + cq], s);
+                                s = make_float4(0.f, 0.f, 0.f, 0.f);
+                                ++r;
+                                r_end = rst[r + 1];
+                            }
+                            if (col_ok) s = fma4(vv[u], xv[u], s);
+                        }
+                    }
+                }
+                if (e_hi > e_lo) ys4[r * CQ + cq] = add4(ys4[r * CQ + cq], s);   // the last entry's row
+            }
+        } else
         for (int r = act ? s_wrow[warp] : 0; r < (act ? s_wrow[warp + 1] : 0); ++r) {
             const int b = rst[r], e = rst[r + 1];
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int base = b; base < e; base += RSUB) {
-                const int i = base + rs;
-                if (i < e && col_ok) {
-                    const uint2 en = __ldg(E + i);
-                    s = fma4(__uint_as_float(en.x),
-                             __ldg(reinterpret_cast<const float4 *>(X + (int64_t)en.y * a.ldx + n0 + 4 * cq)), s);
+            for (int c0 = b; c0 < e; c0 += 32) {
+                const int cnt = min(32, e - c0);
+                const uint2 mine = lane < cnt ? __ldg(E + c0 + lane) : make_uint2(0u, 0u);
+                for (int k0 = 0; k0 < cnt; k0 += CSR_U * RSUB) {
+                    float4 xv[CSR_U];
+                    float vv[CSR_U];
+#pragma unroll
+                    for (int u = 0; u < CSR_U; ++u) {
+                        const int k = k0 + u * RSUB + rs;
+                        const int src = k < 32 ? k : 31;
+                        vv[u] = __uint_as_float(__shfl_sync(FULL, mine.x, src));
+                        const uint32_t col = __shfl_sync(FULL, mine.y, src);
+                        xv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (k < cnt && col_ok)
+                            xv[u] = __ldg(reinterpret_cast<const float4 *>(X + (int64_t)col * a.ldx + n0 + 4 * cq));
+                    }
+#pragma unroll
+                    for (int u = 0; u < CSR_U; ++u)
+                        if (k0 + u * RSUB + rs < cnt && col_ok) s = fma4(vv[u], xv[u], s);
                 }
             }
 #pragma unroll
