@@ -37,7 +37,8 @@ def _sources() -> list[pathlib.Path]:
 
 def _fingerprint(srcs: list[pathlib.Path]) -> str:
     h = hashlib.sha256()
-    for p in [*srcs, *CSRC.glob("*.h"), *INCLUDE.glob("*.h"), pathlib.Path(__file__)]:
+    for p in [*srcs, *sorted(CSRC.glob("*.h")), *sorted(CSRC.glob("*.cuh")), *sorted(INCLUDE.glob("*.h")),
+              pathlib.Path(__file__)]:
         h.update(p.name.encode())
         h.update(p.read_bytes())
     return h.hexdigest()

@@ -31,6 +31,17 @@ __device__ __forceinline__ void mbar_init(unsigned bar) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
 }
 
+// An mbarrier whose phase completes after `count` arrivals.
+__device__ __forceinline__ void mbar_init_count(unsigned bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count) : "memory");
+}
+
+// One arrival (release at CTA scope: this thread's earlier writes, and those
+// ordered before it, are visible to a thread whose wait sees the phase end).
+__device__ __forceinline__ void mbar_arrive(unsigned bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
+}
+
 // Wait for phase `parity` of an mbarrier, giving up after WAIT_NS.
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
     unsigned done = 0;

@@ -117,12 +117,11 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
     constexpr int UPT = (UNITS + SABLE_THREADS - 1) / SABLE_THREADS; // per thread
     constexpr int NPROD = TERMS == 3 ? 6 : 3;
     __shared__ __align__(8) uint64_t s_full[UMMA_BST_MAX];   // panel copy of a stage landed
+    __shared__ __align__(8) uint64_t s_afull[2];         // X terms of the step of that parity written (8 warps)
     __shared__ __align__(8) uint64_t s_done[2];          // products of steps of that parity completed
     __shared__ uint32_t s_taddr;
-    // abort flags: [ks & 1] is written before and read after the barrier of
-    // step ks (a thread already in step ks + 1 writes the other one), [2]
-    // after the K loop
-    __shared__ int s_abort[3];
+    __shared__ int s_stop;        // a bounded wait ran out: every loop stops at its next check
+    __shared__ int s_committed;   // steps whose products the issuer committed
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool prod = tid < SABLE_THREADS;          // producer threads
@@ -149,8 +148,11 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
             for (int s = 0; s < bst; ++s) mbar_init(smem_addr(&s_full[s]));
             mbar_init(smem_addr(&s_done[0]));
             mbar_init(smem_addr(&s_done[1]));
+            mbar_init_count(smem_addr(&s_afull[0]), SABLE_THREADS / 32);
+            mbar_init_count(smem_addr(&s_afull[1]), SABLE_THREADS / 32);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-            s_abort[0] = s_abort[1] = s_abort[2] = 0;
+            s_stop = 0;
+            s_committed = 0;
         }
         if (warp == 0) tmem_alloc(smem_addr(&s_taddr), ncols);
         tc_fence_before();
@@ -181,101 +183,124 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                     dst[i] = ld_pinned_f4(X + (int64_t)row * a.ldx + n);
             }
         };
-        bool bad = false;       // issuer: a panel copy wait ran out (published before the next barrier)
-        int issued = look < nks ? look : nks, landed = 0;   // issuer: panel copies
-        int steps_run = nks;    // steps whose products were committed (uniform across the CTA)
-        // Step ks: its X values are in `slot` (loaded two steps earlier), which
-        // then receives those of step ks + 2, whose row `cm` was read two steps
-        // earlier still; `cm` then receives the row of step ks + 4.  false:
-        // the CTA stops (abort; uniform).
-        auto step = [&](int ks, float4 (&slot)[UPT], int &cm) -> bool {
-            // the products of step ks - 2 have read their A stage (ks & 1) and
-            // their panel stage ((ks + look) % bst)
-            if (ks >= 2 && !mbar_wait(smem_addr(&s_done[ks & 1]), (uint32_t)(((ks - 2) >> 1) & 1))) s_abort[ks & 1] = 1;
-            if (issuer) {
-                if (bad) s_abort[ks & 1] = 1;
+        // The producer warps and the issuer run decoupled and hand the stages
+        // over through mbarriers: a producer warp writes its part of the X
+        // terms of step ks, fences them to the async proxy and arrives on
+        // s_afull[ks & 1] (the eight warps' arrivals complete the phase); the
+        // issuer waits for that and for the step's panel copy, issues the
+        // products and commits them to s_done[ks & 1], on which the producers
+        // (before they reuse the X stage) and the issuer (before it reuses
+        // the panel stage) wait two steps later.  Neither side waits for the
+        // other's issue work, only for the data it needs.  A wait that runs
+        // out sets s_stop, which both loops check, so an error ends the item
+        // after at most one more bounded wait per thread.
+        if (prod) {
+            float4 xr0[UPT], xr1[UPT];   // X values of the next even / odd step
+            load_step(col_row(0), xr0);
+            load_step(col_row(1), xr1);
+            int cm0 = col_row(2), cm1 = col_row(3);
+            // Step ks: its X values are in `slot` (loaded two steps earlier),
+            // which then receives those of step ks + 2, whose row `cm` was read
+            // two steps earlier still; `cm` then receives the row of step
+            // ks + 4.  false: stop (warp-uniform).
+            auto pstep = [&](int ks, float4 (&slot)[UPT], int &cm) -> bool {
+                if (ks >= 2) {   // the products of step ks - 2 have read this X stage
+                    const bool ok = mbar_wait(smem_addr(&s_done[ks & 1]), (uint32_t)(((ks - 2) >> 1) & 1));
+                    const bool stop = *reinterpret_cast<volatile int *>(&s_stop) != 0;
+                    if (__any_sync(FULL, !ok || stop)) {
+                        if (!ok) s_stop = 1;
+                        return false;
+                    }
+                }
+                float4 cur[UPT];
+#pragma unroll
+                for (int i = 0; i < UPT; ++i) cur[i] = slot[i];
+                load_step(cm, slot);
+                cm = col_row(ks + 4);
+                unsigned char *As = smem + L::OFF_A + (ks & 1) * L::A_STAGE;
+#pragma unroll
+                for (int i = 0; i < UPT; ++i) {
+                    const int u = tid + i * SABLE_THREADS;
+                    if (u < UNITS) {
+                        int k, q;
+                        umma_unit(u, k, q);
+                        uint2 t[TERMS];
+                        split4<TERMS>(cur[i], t);
+                        const int off = umma_mnmajor_off(4 * q, k);
+#pragma unroll
+                        for (int e = 0; e < TERMS; ++e) *reinterpret_cast<uint2 *>(As + e * (UMMA_M * 32) + off) = t[e];
+                    }
+                }
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(smem_addr(&s_afull[ks & 1]));
+                return true;
+            };
+            for (int ks = 0; ks < nks; ks += 2) {
+                if (!pstep(ks, xr0, cm0)) break;
+                if (ks + 1 < nks && !pstep(ks + 1, xr1, cm1)) break;
+            }
+        } else if (issuer) {
+            int issued = look < nks ? look : nks, landed = 0, committed = 0;
+            for (int ks = 0; ks < nks; ++ks) {
+                if (*reinterpret_cast<volatile int *>(&s_stop)) break;
+                // the products of step ks - 2 have read the panel stage that
+                // step ks + look takes
+                if (ks >= 2 && !mbar_wait(smem_addr(&s_done[ks & 1]), (uint32_t)(((ks - 2) >> 1) & 1))) {
+                    s_stop = 1;
+                    break;
+                }
                 const int j = ks + look;
                 if (j < nks) {
                     tma_record(smem_addr(&s_full[j % bst]), smem + L::OFF_B + (j % bst) * bstage,
                                planes + (size_t)j * step_src, copy_bytes);
                     issued = j + 1;
                 }
-            }
-            float4 cur[UPT];
-#pragma unroll
-            for (int i = 0; i < UPT; ++i) cur[i] = slot[i];
-            load_step(cm, slot);
-            cm = col_row(ks + 4);
-            unsigned char *As = smem + L::OFF_A + (ks & 1) * L::A_STAGE;
-#pragma unroll
-            for (int i = 0; i < UPT; ++i) {
-                const int u = tid + i * SABLE_THREADS;
-                if (prod && u < UNITS) {
-                    int k, q;
-                    umma_unit(u, k, q);
-                    uint2 t[TERMS];
-                    split4<TERMS>(cur[i], t);
-                    const int off = umma_mnmajor_off(4 * q, k);
-#pragma unroll
-                    for (int e = 0; e < TERMS; ++e) *reinterpret_cast<uint2 *>(As + e * (UMMA_M * 32) + off) = t[e];
-                }
-            }
-            fence_async_smem();
-            __syncthreads();
-            if (s_abort[ks & 1]) {
-                steps_run = ks;
-                return false;
-            }
-            if (issuer) {
                 const int s = ks % bst;
-                if (mbar_wait(smem_addr(&s_full[s]), (uint32_t)((ks / bst) & 1))) {
-                    landed = ks + 1;
-                    tc_fence_after();
-                    const uint32_t a_st = a_base + (uint32_t)((ks & 1) * L::A_STAGE);
-                    const uint32_t b_st = b_base + (uint32_t)(s * bstage);
-                    // products (x term, panel term), smallest first
-                    constexpr int PA[6] = {1, 0, 2, 0, 1, 0}, PB[6] = {1, 2, 0, 1, 0, 0};
-                    constexpr int QA[3] = {0, 1, 0}, QB[3] = {1, 0, 0};
+                if (!mbar_wait(smem_addr(&s_afull[ks & 1]), (uint32_t)((ks >> 1) & 1))) {
+                    s_stop = 1;
+                    break;
+                }
+                if (!mbar_wait(smem_addr(&s_full[s]), (uint32_t)((ks / bst) & 1))) {
+                    s_stop = 1;
+                    break;
+                }
+                landed = ks + 1;
+                tc_fence_after();
+                const uint32_t a_st = a_base + (uint32_t)((ks & 1) * L::A_STAGE);
+                const uint32_t b_st = b_base + (uint32_t)(s * bstage);
+                // products (x term, panel term), smallest first
+                constexpr int PA[6] = {1, 0, 2, 0, 1, 0}, PB[6] = {1, 2, 0, 1, 0, 0};
+                constexpr int QA[3] = {0, 1, 0}, QB[3] = {1, 0, 0};
 #pragma unroll
-                    for (int p = 0; p < NPROD; ++p) {
-                        const int ta = TERMS == 3 ? PA[p] : QA[p], tb = TERMS == 3 ? PB[p] : QB[p];
-                        const uint64_t ad = umma_sdesc(a_st + (uint32_t)(ta * UMMA_M * 32), UMMA_MN_LBO, UMMA_MN_SBO);
-                        const uint64_t bd = umma_sdesc(b_st + (uint32_t)(tb * hp * 32), UMMA_KM_LBO, UMMA_KM_SBO);
-                        umma_bf16(taddr, ad, bd, idesc, (ks > 0 || p > 0) ? 1u : 0u);
-                    }
-                } else {
-                    bad = true;
+                for (int p = 0; p < NPROD; ++p) {
+                    const int ta = TERMS == 3 ? PA[p] : QA[p], tb = TERMS == 3 ? PB[p] : QB[p];
+                    const uint64_t ad = umma_sdesc(a_st + (uint32_t)(ta * UMMA_M * 32), UMMA_MN_LBO, UMMA_MN_SBO);
+                    const uint64_t bd = umma_sdesc(b_st + (uint32_t)(tb * hp * 32), UMMA_KM_LBO, UMMA_KM_SBO);
+                    umma_bf16(taddr, ad, bd, idesc, (ks > 0 || p > 0) ? 1u : 0u);
                 }
                 umma_commit(smem_addr(&s_done[ks & 1]));
+                committed = ks + 1;
             }
-            return true;
-        };
-        float4 xr0[UPT], xr1[UPT];   // X values of the next even / odd step
-        load_step(col_row(0), xr0);
-        load_step(col_row(1), xr1);
-        int cm0 = col_row(2), cm1 = col_row(3);
-        for (int ks = 0; ks < nks; ks += 2) {
-            if (!step(ks, xr0, cm0)) break;
-            if (ks + 1 < nks && !step(ks + 1, xr1, cm1)) break;
+            // every panel copy issued has landed before the CTA exits
+            for (int j = landed; j < issued; ++j)
+                if (!mbar_wait(smem_addr(&s_full[j % bst]), (uint32_t)((j / bst) & 1))) s_stop = 1;
+            s_committed = committed;
         }
+        __syncthreads();
+        const int committed = s_committed;
         // Every product issued has completed before TMEM is read or freed:
         // a commit tracks the MMAs issued since the previous commit, and the
         // MMAs of one accumulator complete in issue order, so the last step's
-        // commit covers them all.  Every panel copy issued has landed before
-        // the CTA exits.
-        if (issuer) {
-            if (bad) s_abort[2] = 1;
-            for (int j = landed; j < issued; ++j)
-                if (!mbar_wait(smem_addr(&s_full[j % bst]), (uint32_t)((j / bst) & 1))) s_abort[2] = 1;
-        }
-        if (steps_run > 0) {
-            const int last = steps_run - 1;
-            if (!mbar_wait(smem_addr(&s_done[last & 1]), (uint32_t)((last >> 1) & 1))) s_abort[2] = 1;
+        // commit covers them all.
+        if (committed > 0) {
+            const int last = committed - 1;
+            if (!mbar_wait(smem_addr(&s_done[last & 1]), (uint32_t)((last >> 1) & 1))) s_stop = 1;
         }
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
-        if (s_abort[0] | s_abort[1] | s_abort[2]) {
+        if (s_stop || committed < nks) {
             if (tid == 0) atomicExch(error, 1);
         } else {
             // lane m of quadrant (warp & 3) -> Y column n0 + m; the two warp

@@ -428,10 +428,6 @@ __device__ __forceinline__ WarpSmem warp_smem(unsigned char *base, int stage_byt
     return s;
 }
 
-__device__ __forceinline__ void mbar_init_count(unsigned bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(bar), "r"(count) : "memory");
-}
-
 // Gather (cp.async) every x value of the record: xg[0, 4nq) panel columns,
 // xg[4nq, 4nq + ns) CSR entries, by lanes 0-30.  Completion is counted on
 // the mbarrier xbar (32 arrivals per phase): each gathering lane arrives when
