@@ -45,19 +45,26 @@
 namespace {
 
 constexpr int UMMA_BST_MIN = 4, UMMA_BST_MAX = 8;   // panel-term stages (bulk-copy ring)
+// X-term stages: the producers run up to NA - 1 steps ahead of the MMAs.
+// Two: a third stage takes the shared memory of two panel stages at three
+// CTAs per SM, and the shorter panel-copy lookahead lost more than the
+// producers gained (50000^2, N = 128: 0.1247 ms with two, 0.1280 with three,
+// 0.1471 with four).
+constexpr int UMMA_NA = 2;
 constexpr int UMMA_M = 128;                 // MMA rows (TMEM lanes)
 constexpr int UMMA_THREADS = SABLE_THREADS + 32;   // producers + the issuer warp
 // Dynamic shared memory of one CTA when three CTAs share an SM (228 KB less
 // the per-CTA reserve and static shared memory).
 constexpr int UMMA_SMEM_BUDGET = 75776;
 
-// Shared memory of a CTA: 2 stages of X terms, bst stages of panel terms of
-// bstage bytes, then the CSR row starts; the Y tile reuses the stage space.
+// Shared memory of a CTA: UMMA_NA stages of X terms, bst stages of panel
+// terms of bstage bytes, then the CSR row starts; the Y tile reuses the stage
+// space.
 template <int NT, int TERMS>
 struct UmmaSmem {
     static constexpr int A_STAGE = TERMS * UMMA_M * 32;       // X terms of one step (MN-major, 128 rows)
-    static constexpr int OFF_A = 0;                           // 2 stages
-    static constexpr int OFF_B = OFF_A + 2 * A_STAGE;         // bst stages
+    static constexpr int OFF_A = 0;                           // UMMA_NA stages
+    static constexpr int OFF_B = OFF_A + UMMA_NA * A_STAGE;   // bst stages
     static constexpr int YS = SABLE_MAX_ROW_TILE * NT * 4;    // Y tile (after the K loop, over the stages)
     static constexpr int RST = (SABLE_MAX_ROW_TILE + 8) * 4;
     __host__ __device__ static constexpr int off_rst(int bst, int bstage) {
@@ -117,8 +124,8 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
     constexpr int UPT = (UNITS + SABLE_THREADS - 1) / SABLE_THREADS; // per thread
     constexpr int NPROD = TERMS == 3 ? 6 : 3;
     __shared__ __align__(8) uint64_t s_full[UMMA_BST_MAX];   // panel copy of a stage landed
-    __shared__ __align__(8) uint64_t s_afull[2];         // X terms of the step of that parity written (8 warps)
-    __shared__ __align__(8) uint64_t s_done[2];          // products of steps of that parity completed
+    __shared__ __align__(8) uint64_t s_afull[UMMA_NA];   // X terms of stage ks % NA written (8 warp arrivals)
+    __shared__ __align__(8) uint64_t s_done[UMMA_NA];    // products of the step of stage ks % NA completed
     __shared__ uint32_t s_taddr;
     __shared__ int s_stop;        // a bounded wait ran out: every loop stops at its next check
     __shared__ int s_committed;   // steps whose products the issuer committed
@@ -146,10 +153,10 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         const float *__restrict__ X = a.x;
         if (tid == 0) {
             for (int s = 0; s < bst; ++s) mbar_init(smem_addr(&s_full[s]));
-            mbar_init(smem_addr(&s_done[0]));
-            mbar_init(smem_addr(&s_done[1]));
-            mbar_init_count(smem_addr(&s_afull[0]), SABLE_THREADS / 32);
-            mbar_init_count(smem_addr(&s_afull[1]), SABLE_THREADS / 32);
+            for (int s = 0; s < UMMA_NA; ++s) {
+                mbar_init(smem_addr(&s_done[s]));
+                mbar_init_count(smem_addr(&s_afull[s]), SABLE_THREADS / 32);
+            }
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             s_stop = 0;
             s_committed = 0;
@@ -185,12 +192,14 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         };
         // The producer warps and the issuer run decoupled and hand the stages
         // over through mbarriers: a producer warp writes its part of the X
-        // terms of step ks, fences them to the async proxy and arrives on
-        // s_afull[ks & 1] (the eight warps' arrivals complete the phase); the
-        // issuer waits for that and for the step's panel copy, issues the
-        // products and commits them to s_done[ks & 1], on which the producers
-        // (before they reuse the X stage) and the issuer (before it reuses
-        // the panel stage) wait two steps later.  Neither side waits for the
+        // terms of step ks into stage ks % NA, fences them to the async proxy
+        // and arrives on s_afull[ks % NA] (the eight warps' arrivals complete
+        // the phase); the issuer waits for that and for the step's panel copy,
+        // issues the products and commits them to s_done[ks % NA], on which
+        // the producers wait NA steps later (before they reuse the X stage)
+        // and the issuer two steps later (before it reuses the panel stage;
+        // step ks - 2's barrier is s_done[(ks - 2) % NA]).  Phases: step ks
+        // is phase (ks / NA) & 1 of its stage's barriers.  Neither side waits for the
         // other's issue work, only for the data it needs.  A wait that runs
         // out sets s_stop, which both loops check, so an error ends the item
         // after at most one more bounded wait per thread.
@@ -204,8 +213,8 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
             // two steps earlier still; `cm` then receives the row of step
             // ks + 4.  false: stop (warp-uniform).
             auto pstep = [&](int ks, float4 (&slot)[UPT], int &cm) -> bool {
-                if (ks >= 2) {   // the products of step ks - 2 have read this X stage
-                    const bool ok = mbar_wait(smem_addr(&s_done[ks & 1]), (uint32_t)(((ks - 2) >> 1) & 1));
+                if (ks >= UMMA_NA) {   // the products of step ks - NA have read this X stage
+                    const bool ok = mbar_wait(smem_addr(&s_done[ks % UMMA_NA]), (uint32_t)(((ks - UMMA_NA) / UMMA_NA) & 1));
                     const bool stop = *reinterpret_cast<volatile int *>(&s_stop) != 0;
                     if (__any_sync(FULL, !ok || stop)) {
                         if (!ok) s_stop = 1;
@@ -217,7 +226,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 for (int i = 0; i < UPT; ++i) cur[i] = slot[i];
                 load_step(cm, slot);
                 cm = col_row(ks + 4);
-                unsigned char *As = smem + L::OFF_A + (ks & 1) * L::A_STAGE;
+                unsigned char *As = smem + L::OFF_A + (ks % UMMA_NA) * L::A_STAGE;
 #pragma unroll
                 for (int i = 0; i < UPT; ++i) {
                     const int u = tid + i * SABLE_THREADS;
@@ -233,7 +242,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 }
                 fence_async_smem();
                 __syncwarp();
-                if (lane == 0) mbar_arrive(smem_addr(&s_afull[ks & 1]));
+                if (lane == 0) mbar_arrive(smem_addr(&s_afull[ks % UMMA_NA]));
                 return true;
             };
             for (int ks = 0; ks < nks; ks += 2) {
@@ -246,7 +255,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 if (*reinterpret_cast<volatile int *>(&s_stop)) break;
                 // the products of step ks - 2 have read the panel stage that
                 // step ks + look takes
-                if (ks >= 2 && !mbar_wait(smem_addr(&s_done[ks & 1]), (uint32_t)(((ks - 2) >> 1) & 1))) {
+                if (ks >= 2 && !mbar_wait(smem_addr(&s_done[(ks - 2) % UMMA_NA]), (uint32_t)(((ks - 2) / UMMA_NA) & 1))) {
                     s_stop = 1;
                     break;
                 }
@@ -257,7 +266,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                     issued = j + 1;
                 }
                 const int s = ks % bst;
-                if (!mbar_wait(smem_addr(&s_afull[ks & 1]), (uint32_t)((ks >> 1) & 1))) {
+                if (!mbar_wait(smem_addr(&s_afull[ks % UMMA_NA]), (uint32_t)((ks / UMMA_NA) & 1))) {
                     s_stop = 1;
                     break;
                 }
@@ -267,7 +276,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 }
                 landed = ks + 1;
                 tc_fence_after();
-                const uint32_t a_st = a_base + (uint32_t)((ks & 1) * L::A_STAGE);
+                const uint32_t a_st = a_base + (uint32_t)((ks % UMMA_NA) * L::A_STAGE);
                 const uint32_t b_st = b_base + (uint32_t)(s * bstage);
                 // products (x term, panel term), smallest first
                 constexpr int PA[6] = {1, 0, 2, 0, 1, 0}, PB[6] = {1, 2, 0, 1, 0, 0};
@@ -279,7 +288,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                     const uint64_t bd = umma_sdesc(b_st + (uint32_t)(tb * hp * 32), UMMA_KM_LBO, UMMA_KM_SBO);
                     umma_bf16(taddr, ad, bd, idesc, (ks > 0 || p > 0) ? 1u : 0u);
                 }
-                umma_commit(smem_addr(&s_done[ks & 1]));
+                umma_commit(smem_addr(&s_done[ks % UMMA_NA]));
                 committed = ks + 1;
             }
             // every panel copy issued has landed before the CTA exits
@@ -295,7 +304,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         // commit covers them all.
         if (committed > 0) {
             const int last = committed - 1;
-            if (!mbar_wait(smem_addr(&s_done[last & 1]), (uint32_t)((last >> 1) & 1))) s_stop = 1;
+            if (!mbar_wait(smem_addr(&s_done[last % UMMA_NA]), (uint32_t)((last / UMMA_NA) & 1))) s_stop = 1;
         }
         tc_fence_before();
         __syncthreads();
