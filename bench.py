@@ -270,13 +270,16 @@ def bench_batch(reps: int, cpu: bool = True) -> dict:
         xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
         ys.append(torch.empty(m.n_rows if w == 1 else (m.n_rows, w), device="cuda"))
     from oracle import oracle
+    from sable_gb300 import metrics
     plain, learned_comps = [], []
     errs_med = []
     nnz_work = 0
+    bytes_work = 0   # algorithmic bytes of all 256 products (memory bound of the batch)
     for m, w in zip(mats, widths):
         bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
         f, rf, mlp = choices(m, bt, w)
         nnz_work += int(f[:, 2].sum()) * w
+        bytes_work += metrics.spmv_bytes(m) if w == 1 else metrics.spmm_bytes(m, w)
         lay = "mixed" if w == 1 else "separate"
         plain.append(Plan(convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, rf, bt=bt),
                           split_layout=lay))
@@ -336,6 +339,13 @@ def bench_batch(reps: int, cpu: bool = True) -> dict:
             "plain_ms": round(ms_p, 4), "plain_launches": len(mats) + sum(1 for w in widths if w == 1),
             "learned_batched_ms": round(ms_b, 4), "learned_vs_plain": round(ms_p / ms_b, 3),
             "work_gflop": round(2 * nnz_work / 1e9, 3), "learned_batched_gflops": round(2 * nnz_work / (ms_b * 1e6), 1),
+            "roofline": {"bound": "hbm", "achieved": round(bytes_work / (ms_b * 1e-3) / 1e9, 1),
+                         "peak": peaks()["hbm_gbs"], "unit": "GB/s",
+                         "frac": round(bytes_work / (ms_b * 1e-3) / 1e9 / peaks()["hbm_gbs"], 4),
+                         "bytes_per_run": int(bytes_work),
+                         "note": "algorithmic bytes of the 256 products (each block at its cheaper FP32 encoding, "
+                                 "x/X read once, y/Y written once) / batch time; the SpMM half is also bound by "
+                                 "the split-BF16 tensor work (six products per dense value)"},
             "error_vs_fp64_scaled": {"max": float(np.max(errs)), "median": float(np.median(errs_med)),
                                      "matrices": len(errs), "tolerance": oracle.TOL,
                                      "measure": "per output |y - y_fp64| / (|A||x|), all 256 matrices"},
@@ -369,6 +379,41 @@ def run_spmm_profile(args):
     plan.check()
     print(json.dumps({"spmm_profile": {"N": N, "row_tile": rt, "chunk_bytes": cb, "items": plan.stats()["n_chunks"],
                                        "ms_per_launch": s.elapsed_time(e) / args.steps}}))
+
+
+def run_batch_profile(args):
+    """The 256-matrix batch with the learned choice in the batch autotuner's
+    usual shapes (per-warp SpMV plans, 16-row tiles, 32 KB items; SpMM plans
+    with whole block rows), a few graph launches, nothing else (for kernel
+    profiles and launch lists)."""
+    import torch
+    from sable_gb300 import autotune, convert, synth
+    from sable_gb300.batch import Batch
+    mats, widths = synth.batch_256()
+    rng = np.random.default_rng(0)
+    plans, xs, ys = [], [], []
+    for m, w in zip(mats, widths):
+        bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+        _, _, mlp = choices(m, bt, w)
+        comp = convert.compress(m.val, m.rpntr, m.cpntr, m.indx, m.bindx, m.bpntrb, m.bpntre, mlp, bt=bt)
+        shape = autotune.BATCH_SPMV_SHAPES[0] if w == 1 else autotune.BATCH_SPMM_SHAPES[0]
+        plans.append(autotune._batch_plan(comp, shape, w, "split3"))
+        xs.append(torch.as_tensor(rng.uniform(-1, 1, m.n_cols if w == 1 else (m.n_cols, w)).astype(np.float32)).cuda())
+        ys.append(torch.empty(m.n_rows if w == 1 else (m.n_rows, w), device="cuda"))
+    b = Batch(plans, widths, use_graph=True)
+    for p in plans:
+        p.close()
+    for _ in range(args.warmup):
+        b.run(xs, ys)
+    s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record()
+    for _ in range(args.steps):
+        b.run(xs, ys)
+    e0.record()
+    e0.synchronize()
+    b.check()
+    print(json.dumps({"batch_profile": {"ms_per_run": s0.elapsed_time(e0) / args.steps, **b.info()}}))
+    b.close()
 
 
 def run_sable(args):
@@ -582,6 +627,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="headline SpMV only (no SpMM / batch sections)")
     ap.add_argument("--spmm-profile", help="N,ROW_TILE,CHUNK_BYTES: only run the 50000^2 SpMM (learned choice, "
                                            "split BF16) in this shape, for kernel profiles")
+    ap.add_argument("--batch-profile", action="store_true", help="only run the 256-matrix batch in the autotuner's "
+                                                                 "usual shapes (for kernel profiles)")
     ap.add_argument("--shape", help="ROW_TILE,CHUNK_BYTES: run the headline on the per-warp executor in this shape "
                                     "instead of autotuning (for kernel profiles)")
     args = ap.parse_args()
@@ -591,6 +638,8 @@ def main():
         run_reference(args)
     elif args.spmm_profile:
         run_spmm_profile(args)
+    elif args.batch_profile:
+        run_batch_profile(args)
     else:
         run_sable(args)
 
