@@ -200,16 +200,19 @@ int sable_spmm_timed(sable_plan *plan, const float *X_dev, float *Y_dev, int32_t
 int sable_plan_chunk_tiles(const sable_plan *plan, int64_t *tile_of_chunk);
 
 /*
- * Batch: many plans (matrices) executed by one persistent kernel over a
- * shared work queue.  No reference counterpart (the reference times one
- * matrix per process).  widths[i] = 1 runs SpMV on plan i; widths[i] = N > 1
- * (N % 4 == 0) runs SpMM of width N, on the tensor cores when plan i was
- * created with spmm_tc and N >= 32.  Work units are (item, N-slice) pairs of
- * every plan, sorted by class (split-BF16 SpMM, FP32 SpMM, SpMV) and, within
- * a class, by size, largest first; persistent CTAs take units in that order
- * from an atomic queue head and keep several SpMV records in flight (TMA
- * ring of `stages` records per CTA).  The batch copies the plans' records; the
- * plans may be destroyed after sable_batch_create.
+ * Batch: many plans (matrices) run together, one graph launch per run.  No
+ * reference counterpart (the reference times one matrix per process).
+ * widths[i] = 1 runs SpMV on plan i; widths[i] = N > 1 (N % 4 == 0) runs SpMM
+ * of width N, on the tensor cores when plan i was created with spmm_tc and
+ * N >= 32.  Each matrix goes to the fastest executor its plan allows:
+ * split-BF16 SpMM of plans with tcgen05 panel terms to the tcgen05 kernel
+ * (one launch per N-slice width over the items of all of them, largest
+ * first), SpMV of per-warp plans (schedule 2) to the per-warp kernel (one
+ * launch over all their items), the rest to a persistent kernel whose CTAs
+ * take (item, N-slice) units from an atomic queue sorted by class (split-BF16
+ * SpMM, FP32 SpMM, SpMV) and size, keeping several SpMV records in flight
+ * (TMA ring of `stages` records per CTA).  The batch copies the plans'
+ * records; the plans may be destroyed after sable_batch_create.
  */
 typedef struct sable_batch_opts {
     int32_t ctas_per_sm;  /* persistent CTAs per SM (0: as many as fit)       */
@@ -222,7 +225,8 @@ typedef struct sable_batch_opts {
 typedef struct sable_batch_info {
     int32_t n_mats;
     int32_t n_ctas;           /* persistent CTAs of the launch               */
-    int64_t n_units;          /* work units in the queue                     */
+    int64_t n_units;          /* work units: tcgen05 (item, slice) pairs,
+                                 per-warp items and the queue's units        */
     int64_t device_bytes;     /* records, tables and scratch of the batch    */
     int32_t smem_bytes;       /* dynamic shared memory per CTA               */
     int32_t stage_bytes;      /* TMA staging bytes per SpMV stage            */
@@ -232,8 +236,9 @@ typedef struct sable_batch_info {
 int sable_batch_create(sable_plan *const *plans, int32_t n_plans, const int32_t *widths,
                        const sable_batch_opts *opts, sable_batch **out);
 /* x_devs[i] / y_devs[i]: operand and result of matrix i, row-major with
- * leading dimension N (SpMM: 16-byte aligned).  One kernel launch (or one
- * graph launch) for the whole batch, stream-ordered on `stream`. */
+ * leading dimension N (SpMM: 16-byte aligned).  One graph launch for the
+ * whole batch (without use_graph, its launches in a row), stream-ordered on
+ * `stream`. */
 int sable_batch_run(sable_batch *batch, const float *const *x_devs, float *const *y_devs, void *stream);
 /* Synchronises `stream`; SABLE_ERR_TIMEOUT if a bounded wait ran out. */
 int sable_batch_check(sable_batch *batch, void *stream);
