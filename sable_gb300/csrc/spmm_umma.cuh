@@ -22,8 +22,9 @@
 //              blocks of hp x 32 bytes (hp = h rounded up to 16); one bulk
 //              copy (cp.async.bulk, mbarrier completion) brings TERMS of them
 //              into a ring of bst stages, bst - 2 steps ahead of the MMAs
-//              (bst = 4..8, as many stages of the plan's tallest tile as fit
-//              beside three CTAs per SM; LaunchArgs.umma_bst / umma_bstage).
+//              (the launch sizes the ring for 4..8 stages of its tallest
+//              tile beside three CTAs per SM; an item with shorter tiles fits
+//              more of its own stages in the same bytes, up to 8).
 //   A operand  the 16 X rows of the step (NT floats each, from L2), loaded
 //              two steps ahead into registers with 16-byte loads (their row
 //              indices four steps ahead, so no load waits on another), split
@@ -114,11 +115,12 @@ __device__ __forceinline__ void umma_unit(int u, int &k, int &q) {
 }
 
 // planes: the item's panel terms (3 term blocks of hp x 32 bytes per step);
-// bst / bstage: the panel ring (stages, bytes per stage >= TERMS hp 32).
+// ring_bst / ring_bstage: the launch's panel ring (stages of its tallest
+// tile, bytes per stage >= TERMS hp 32).
 template <int NT, int TERMS>
 __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const MatIO &a, int slice, int64_t part_stride,
-                                               unsigned char *smem, const unsigned char *planes, int *error, int bst,
-                                               int bstage) {
+                                               unsigned char *smem, const unsigned char *planes, int *error,
+                                               int ring_bst, int ring_bstage) {
     using L = UmmaSmem<NT, TERMS>;
     constexpr int UNITS = 4 * NT;                                    // float4 loads per step
     constexpr int UPT = (UNITS + SABLE_THREADS - 1) / SABLE_THREADS; // per thread
@@ -138,12 +140,16 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
     const int n0 = slice * NT;
     float *ys = reinterpret_cast<float *>(smem);
     float4 *ys4 = reinterpret_cast<float4 *>(smem);
-    int *rst = reinterpret_cast<int *>(smem + L::off_rst(bst, bstage));
-    const int look = bst - 2;    // panel copies run this many steps ahead
+    int *rst = reinterpret_cast<int *>(smem + L::off_rst(ring_bst, ring_bstage));
 
     if (nq > 0) {
         const int nks = (ncol + 15) >> 4;
         const int hp = (h + 15) & ~15;
+        // this item's panel stages in the launch's ring bytes (at most
+        // UMMA_BST_MAX): a short tile copies its panel terms further ahead
+        const int bstage = TERMS * hp * 32;
+        const int bst = min(UMMA_BST_MAX, (ring_bst * ring_bstage) / bstage);
+        const int look = bst - 2;    // panel copies run this many steps ahead
         const uint32_t ncols = umma_tmem_cols(hp);
         const uint32_t step_src = 3u * (uint32_t)hp * 32u;           // bytes of a step in `planes`
         const uint32_t copy_bytes = (uint32_t)TERMS * (uint32_t)hp * 32u;
