@@ -61,6 +61,12 @@ struct sable_plan {
     std::vector<int64_t> umma_off_host;  // the same on the host
     int64_t umma_bytes = 0;
     int umma_hp = 16;                    // tallest tile with a panel, rounded up to 16
+    // sable_spmv_host on pinned buffers: the copy of x into the device
+    // staging and the SpMV, captured once as a graph for the last (x, y) pair
+    cudaGraphExec_t host_exec = nullptr;
+    const float *host_x = nullptr;       // mapped x the graph reads
+    float *host_y = nullptr;             // mapped y the graph writes
+    const float *host_dx = nullptr;      // device staging of x the graph copies into
     float *d_ppartial = nullptr;         // multi-part tile partials
     int *d_pcounters = nullptr;          // multi-part tile counters
     int64_t n_parts = 0, n_multi = 0;

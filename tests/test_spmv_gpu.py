@@ -215,6 +215,39 @@ def test_host_entry_pinned_buffers(cuda, schedule):
     plan.check()
 
 
+@pytest.mark.parametrize("schedule", ["items", "warp_items"])
+def test_host_entry_graph_follows_buffers(cuda, schedule):
+    """With both buffers pinned, sable_spmv_host replays a graph of the x
+    copy and the SpMV kept for the last (x, y) pair: alternating between two
+    pinned pairs (the graph is captured again at every change), new x values
+    in the same buffer (replayed as is), a pinned x with a pageable y and a
+    pageable pair (the copy path): always the device-buffer SpMV's bits."""
+    import torch
+    from sable_gb300 import _lib
+    m = synth.spmv_1000()
+    rng = np.random.default_rng(25)
+    plan, comp, y_ref, yabs = plan_and_ref(m, rng.random(m.n_blocks) < 0.5, synth.vector(m.n_cols, 26),
+                                           schedule=schedule, chunk_bytes=4096)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    pairs = [(torch.zeros(m.n_cols).pin_memory(), torch.zeros(m.n_rows).pin_memory()) for _ in range(2)]
+    for k in range(6):
+        xh, yh = pairs[k % 2]
+        x = synth.vector(m.n_cols, 100 + k)
+        xh.copy_(torch.as_tensor(x))
+        yh.fill_(float("nan"))
+        _lib.check(lib.sable_spmv_host(plan.handle, xh.data_ptr(), yh.data_ptr(), stream), "sable_spmv_host")
+        np.testing.assert_array_equal(yh.numpy(), plan.spmv(torch.as_tensor(x).cuda()).cpu().numpy())
+    x = synth.vector(m.n_cols, 200)
+    xp = torch.as_tensor(x).pin_memory()
+    yq = np.full(m.n_rows, np.nan, np.float32)          # pageable
+    _lib.check(lib.sable_spmv_host(plan.handle, xp.data_ptr(), yq.ctypes.data, stream), "sable_spmv_host")
+    y_dev = plan.spmv(torch.as_tensor(x).cuda()).cpu().numpy()
+    np.testing.assert_array_equal(yq, y_dev)
+    np.testing.assert_array_equal(plan.spmv_host(x), y_dev)
+    plan.check()
+
+
 def test_spmv_100k_full_size(cuda):
     """The 100000^2 workload (~20k blocks, ~5e7 stored values) at full size
     against the FP64 oracle, with the learned-form split (dense where the
