@@ -28,13 +28,16 @@
 //   A operand  the 16 X rows of the step (NT floats each, from L2), loaded
 //              two steps ahead into registers with 16-byte loads (their row
 //              indices four steps ahead, so no load waits on another), split
-//              into TERMS BF16 terms by the CTA and stored in the MN-major
-//              layout (8-byte stores, conflict-free) into a ring of 2 stages.
-//   MMA        the issuer waits for the step's panel copy, issues the TERMS
-//              products (tcgen05.mma.cta_group::1.kind::f16, M = 128, N = hp,
-//              K = 16) and commits them to the step parity's mbarrier; the
-//              CTA waits for the products of step ks - 2 before it reuses
-//              their stages.
+//              into TERMS BF16 terms by the producer warps and stored in the
+//              MN-major layout (8-byte stores, conflict-free) into a ring of
+//              UMMA_NA stages; each warp then fences its stores to the async
+//              proxy and arrives on the stage's "X ready" mbarrier.
+//   MMA        the issuer waits for the stage's "X ready" barrier and the
+//              step's panel copy, issues the products (tcgen05.mma.cta_group::1
+//              .kind::f16, M = 128, N = hp, K = 16) and commits them to the
+//              stage's "done" mbarrier; the producers wait on it before they
+//              reuse the X stage, the issuer two steps later before it reuses
+//              the panel stage.  No CTA-wide barrier inside the K loop.
 // After the last step the accumulator is read with tcgen05.ld into the Y
 // tile in shared memory (lane m, column n -> Y[n][m]); TMEM is freed on every
 // path.  Every wait is bounded (WAIT_NS); on expiry the error flag is set, the
