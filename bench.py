@@ -230,10 +230,22 @@ def bench_spmm(reps: int, flush, cpu: bool = True) -> dict:
         scale = np.abs(A64[sel]) @ np.abs(Xh)
         rel = np.abs(Yl[sel] - ref) / np.maximum(scale, 1e-300)
         F = metrics.spmm_flops(m, N)
+        # roofline of the learned form: the larger of its algorithmic bytes at
+        # the measured HBM peak and its useful flops at the measured BF16
+        # tensor peak shared by the six split products
+        pk = peaks()
+        Bm = metrics.spmm_bytes(m, N)
+        t_mem = Bm / (pk["hbm_gbs"] * 1e9)
+        t_tc = F / ((pk["bf16_tflops"] or 1900.0) * 1e12 / 6)
+        roof = {"bound": "hbm" if t_mem >= t_tc else "tensor", "bytes": int(Bm),
+                "time_bound_us": round(max(t_mem, t_tc) * 1e6, 2),
+                "frac": round(max(t_mem, t_tc) / (ms_l * 1e-3), 4),
+                "achieved_gbs": round(Bm / (ms_l * 1e-3) / 1e9, 1), "peak_gbs": pk["hbm_gbs"],
+                "peak_bf16_tflops": pk["bf16_tflops"], "products_per_flop": 6}
         out[f"N{N}"] = {
             "plain_fp32_gflops": round(F / (ms_p * 1e-3) / 1e9, 1), "plain_ms": round(ms_p, 4),
             "learned_tc_gflops": round(F / (ms_l * 1e-3) / 1e9, 1), "learned_ms": round(ms_l, 4),
-            "learned_vs_plain": round(ms_p / ms_l, 3), "learned_config": tuned.config,
+            "learned_vs_plain": round(ms_p / ms_l, 3), "learned_config": tuned.config, "roofline": roof,
             "error_vs_fp64_scaled": {"max": float(rel.max()), "median": float(np.median(rel)), "rows": 4000,
                                      "precision": "split-BF16, three terms (hi+mid+lo), six products, FP32 accum"},
             "dense_frac_learned": round(float(mlp.mean()), 3), "dense_frac_plain": round(float(rf.mean()), 3)}
