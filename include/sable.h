@@ -329,6 +329,15 @@ int sable_mlp_loss_grad(sable_mlp *m, const float *feat_dev, const float *target
 int sable_mlp_train_step(sable_mlp *m, const float *feat_dev, const float *target_dev, const int32_t *idx_dev,
                          int32_t n, float lr, float *loss_dev, void *stream);
 
+/* Self-test of the bounded device waits (no counterpart in the reference):
+ * a one-thread kernel waits up to limit_us (1..2e6) microseconds for an
+ * mbarrier phase; with arrive == 0 nothing completes it, the wait runs out
+ * and the call returns SABLE_ERR_TIMEOUT, as the kernels report a wait that
+ * ran out (the context stays usable); with arrive != 0 the thread arrives
+ * first and the call returns SABLE_OK.  *elapsed_ns (if not NULL): the
+ * time the wait took on the device.  Synchronises `stream`. */
+int sable_selftest_wait(int64_t limit_us, int32_t arrive, int64_t *elapsed_ns, void *stream);
+
 const char *sable_strerror(int code);
 const char *sable_last_error(void);
 /* Library version string. */

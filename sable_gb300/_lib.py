@@ -104,6 +104,7 @@ SIGNATURES = {
     "sable_mlp_infer": (c_int, [c_void_p, c_void_p, c_int32, c_void_p, c_void_p]),
     "sable_mlp_loss_grad": (c_int, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p]),
     "sable_mlp_train_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_float, c_void_p, c_void_p]),
+    "sable_selftest_wait": (c_int, [ctypes.c_int64, c_int32, c_void_p, c_void_p]),
     "sable_strerror": (c_char_p, [c_int]),
     "sable_last_error": (c_char_p, []),
     "sable_version": (c_char_p, []),

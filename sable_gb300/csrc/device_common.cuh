@@ -42,8 +42,8 @@ __device__ __forceinline__ void mbar_arrive(unsigned bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" :: "r"(bar) : "memory");
 }
 
-// Wait for phase `parity` of an mbarrier, giving up after WAIT_NS.
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+// Wait for phase `parity` of an mbarrier, giving up after limit_ns.
+__device__ __forceinline__ bool mbar_wait_for(unsigned bar, unsigned parity, unsigned long long limit_ns) {
     unsigned done = 0;
     const unsigned long long t0 = global_ns();
     while (true) {
@@ -53,9 +53,12 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
             " selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done) : "r"(bar), "r"(parity), "r"(1000000u) : "memory");
         if (done) return true;
-        if (global_ns() - t0 > WAIT_NS) return false;
+        if (global_ns() - t0 > limit_ns) return false;
     }
 }
+
+// Wait for phase `parity` of an mbarrier, giving up after WAIT_NS.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) { return mbar_wait_for(bar, parity, WAIT_NS); }
 
 // Release-acquire arrival on a split-tile counter (one thread, after the
 // partial-sum stores of its CTA / warp are ordered before it).
