@@ -13,7 +13,9 @@ current stream, L2 flushed between runs (L2Flush), median of `reps`.
 The reference fixes its shape per matrix at code-generation time (one C
 function per matrix, src/codegen.py:293-452); this is the GPU counterpart of
 that specialisation step.  Results are cached in memory by a signature of the
-matrix structure and N.
+matrix structure and N.  tune_batch does the same for a batch of matrices:
+it times whole batches over the SpMV matrices' executor and shape, then the
+SpMM matrices' item size, then the ring depth.
 """
 from __future__ import annotations
 

@@ -1,10 +1,11 @@
-// Batched VBR SpMV / SpMM: many matrices, one persistent kernel.
+// Batched VBR SpMV / SpMM: many matrices, one graph launch per run.
 //
 // The reference runs one generated program per matrix; serving many small
 // and mid-size matrices that way leaves the GPU idle between launches and
 // gives every launch its own tail.  A batch merges the item records of all
-// its plans into one device buffer (each record's header carries its matrix
-// index) and builds one work queue of units:
+// its plans into one device buffer (a standard record's header carries its
+// matrix index; compact records get theirs from a per-item table) and builds
+// one work queue of units for the persistent kernel:
 //   SpMV unit   one item record of a width-1 matrix
 //   SpMM unit   one (item record, N-slice) pair, FP32 or split-BF16
 // sorted by class (split-BF16 SpMM, FP32 SpMM, SpMV) and within a class by
@@ -28,8 +29,9 @@
 // phase at a time (the queue order makes the phases disjoint, see the
 // kernel).  Every mbarrier wait is bounded; on expiry the
 // batch's error flag is set and the CTA waits (bounded) for its own copies
-// and leaves.  The SpMV split tiles of all matrices are combined by one
-// launch after the kernel (a second node of the graph).
+// and leaves.  The split tiles of the queue's SpMV matrices are combined by
+// one launch after the kernel.  A run launches only what has work: the
+// tcgen05 launches, the per-warp launch, the persistent kernel, the combine.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
