@@ -26,11 +26,15 @@ out, inside the timed region).  Also reported, each timed the same way:
              choice, one persistent-kernel graph launch
 `--impl reference` times the reference's CPU executor on the headline
 workload: its own generated C (oracle/refc.py: gen_multi_threaded_spmv,
-FP64, OpenMP over the host cores, its compiler flags; about four minutes of
+FP64, OpenMP over the host cores, its compiler flags; a few minutes of
 compilation the first time on a host), or, where those sources were not
-generated, the oracle's C port of it.  The GPU arm's cpu_baseline reports the
-same program when it is already compiled on the host, else the port, for
-the same number of iterations.  Under torchrun each rank runs its own seeded
+generated, the oracle's C port of it; its spmm_50k section times the
+reference's own generated SpMM (gen_multi_threaded_spmm, density 0 as its
+benchmark, FP32, pthreads) at N = 32 and 128, compiled in the same pool.
+The GPU arm's cpu_baseline reports the same SpMV program when it is already
+compiled on the host, else the port, for the same number of iterations; its
+SpMM cpu_baselines run the reference's generated SpMM (compiled on first use
+where the reference arm has not compiled it, about a minute).  Under torchrun each rank runs its own seeded
 replica (weak scaling, no collective on the data path); with --strong the
 ranks instead take block-row shards of the one matrix, balanced by algorithmic
 bytes (sable_gb300.shard), each writing its own rows of y (strong scaling).
@@ -191,7 +195,6 @@ def time_device(fn, steps: int, warmup: int, world: int, flush):
 
 def bench_spmm(reps: int, flush, cpu: bool = True) -> dict:
     """50000^2 SpMM at N = 32 and 128: plain FP32 vs learned split-BF16 (autotuned)."""
-    import scipy.sparse
     import torch
     from sable_gb300 import autotune, convert, metrics, synth
     from sable_gb300.plan import Plan
@@ -215,20 +218,8 @@ def bench_spmm(reps: int, flush, cpu: bool = True) -> dict:
         Yl = Y.cpu().numpy().astype(np.float64)
         # error against FP64 on the host (scipy CSR of A), 4000 sampled rows
         if A64 is None:
-            rows, cols, vals = [], [], []
-            for k in range(len(bt.off)):
-                blk = np.asarray(m.val[bt.off[k]: bt.off[k] + bt.size[k]], np.float64).reshape(bt.w[k], bt.h[k]).T
-                r, c = np.nonzero(blk)
-                rows.append(r + bt.r0[k])
-                cols.append(c + bt.c0[k])
-                vals.append(blk[r, c])
-            A64 = scipy.sparse.csr_array((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
-                                         shape=(m.n_rows, m.n_cols))
-        sel = np.random.default_rng(5).choice(m.n_rows, 4000, replace=False)
-        Xh = X.cpu().numpy().astype(np.float64)
-        ref = A64[sel] @ Xh
-        scale = np.abs(A64[sel]) @ np.abs(Xh)
-        rel = np.abs(Yl[sel] - ref) / np.maximum(scale, 1e-300)
+            A64 = csr64(m, bt)
+        rel = sampled_error(A64, Yl, X.cpu().numpy())
         F = metrics.spmm_flops(m, N)
         # roofline of the learned form: the larger of its algorithmic bytes at
         # the measured HBM peak and its useful flops at the measured BF16
@@ -250,16 +241,66 @@ def bench_spmm(reps: int, flush, cpu: bool = True) -> dict:
                                      "precision": "split-BF16, three terms (hi+mid+lo), six products, FP32 accum"},
             "dense_frac_learned": round(float(mlp.mean()), 3), "dense_frac_plain": round(float(rf.mean()), 3)}
         if cpu:
-            out[f"N{N}"]["cpu_baseline"] = cpu_spmm_baseline(m, X.cpu().numpy(), F)
+            out[f"N{N}"]["cpu_baseline"] = cpu_spmm_baseline(m, X.cpu().numpy(), F, A64)
         plain.close()
         tuned.close()
     return out
 
 
-def cpu_spmm_baseline(m, Xh, F) -> dict:
-    """The oracle's C port of the reference's generated SpMM executor
-    (gen_multi_threaded_spmm: FP32, i-j-k loops per dense block, block rows
-    split over the host cores by LPT), its compiler flags, the full matrix."""
+def csr64(m, bt):
+    """A as an FP64 scipy CSR (for the sampled-row error checks)."""
+    import scipy.sparse
+    rows, cols, vals = [], [], []
+    for k in range(len(bt.off)):
+        blk = np.asarray(m.val[bt.off[k]: bt.off[k] + bt.size[k]], np.float64).reshape(bt.w[k], bt.h[k]).T
+        r, c = np.nonzero(blk)
+        rows.append(r + bt.r0[k])
+        cols.append(c + bt.c0[k])
+        vals.append(blk[r, c])
+    return scipy.sparse.csr_array((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                                  shape=(m.n_rows, m.n_cols))
+
+
+def sampled_error(A64, Y, Xh, rows: int = 4000) -> np.ndarray:
+    """|Y - A X| / (|A||X|) in FP64 over `rows` seeded sampled rows."""
+    sel = np.random.default_rng(5).choice(A64.shape[0], rows, replace=False)
+    Xh = np.asarray(Xh, np.float64)
+    ref = A64[sel] @ Xh
+    scale = np.abs(A64[sel]) @ np.abs(Xh)
+    return np.abs(np.asarray(Y, np.float64)[sel] - ref) / np.maximum(scale, 1e-300)
+
+
+def reference_spmm(N: int, F: float, A64, Xh, runs: int = 4):
+    """The reference's own generated multi-threaded SpMM at width N
+    (oracle/refc.py: gen_multi_threaded_spmm with density 0, as its own
+    benchmark runs it; FP32, its CFLAGS for this host; both widths compiled
+    on first use, about a minute), or None where its sources were not
+    generated.  `runs` timed runs after one dropped cold run."""
+    from oracle import refc
+    if not refc.spmm_generated(N):
+        return None
+    if not refc.spmm_compiled(N):
+        refc.compile((), spmm_widths=[w for w in refc.SPMM_WIDTHS if refc.spmm_generated(w)])
+    r = refc.run_spmm(N, runs + 1)
+    t = np.asarray(r["times_ns"][1:], np.float64) * 1e-9
+    ms = float(np.mean(t)) * 1e3
+    rel = sampled_error(A64, r["Y"], Xh)
+    return {"value": round(F / (ms * 1e-3) / 1e9, 1), "unit": "GFLOP/s", "ms": round(ms, 3),
+            "cores": int(r["threads"]), "kind": "reference",
+            "sample": f"full matrix, width {N}, {len(t)} timed runs after one dropped cold run of the reference's "
+                      f"own generated multi-threaded SpMM (gen_multi_threaded_spmm, density 0 as its benchmark, "
+                      f"{r['threads']} pthreads, FP32, its CFLAGS); max error vs FP64 {float(rel.max()):.1e} of "
+                      f"|A||X| over 4000 sampled rows"}
+
+
+def cpu_spmm_baseline(m, Xh, F, A64) -> dict:
+    """The reference's own generated SpMM (reference_spmm) where its sources
+    were generated, else the oracle's C port of it (gen_multi_threaded_spmm:
+    FP32, i-j-k loops per dense block, block rows split over the host cores
+    by LPT), its compiler flags, the full matrix."""
+    ref = reference_spmm(Xh.shape[1], F, A64, Xh)
+    if ref is not None:
+        return ref
     from oracle import oracle
     threads = os.cpu_count() or 1
     oracle.cpu_spmm_timed(m, Xh, 0, threads, 1)
@@ -552,6 +593,9 @@ def reference_c(steps: int, compile_ok: bool):
     from oracle import oracle, refc
     if not refc.generated() or (not compile_ok and not refc.compiled(("mt",))):
         return None
+    if compile_ok:
+        # the SpMM programs compile in the same pool (the SpMV program takes longest)
+        refc.compile(("mt",), spmm_widths=[w for w in refc.SPMM_WIDTHS if refc.spmm_generated(w)])
     r = refc.run(steps, kinds=("mt",))["mt"]
     m, x, comp = refc._workload()
     y, ya = oracle.spmv_vbrc(comp, x)
@@ -624,7 +668,25 @@ def run_reference(args):
                          "sample": sample},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.quick:
+        out["spmm_50k"] = reference_spmm_section()
     print(json.dumps(out))
+
+
+def reference_spmm_section() -> dict:
+    """The reference's own generated SpMM on the 50000^2 SpMM workload at
+    N = 32 and 128 (reference_spmm), the same widths and operands as the GPU
+    arm's spmm_50k section."""
+    from oracle import refc
+    from sable_gb300 import convert, metrics, synth
+    m = synth.spmm_50k()
+    bt = convert.block_table(m.rpntr, m.cpntr, m.bpntrb, m.bpntre, m.bindx, m.indx)
+    A64 = csr64(m, bt)
+    out = {}
+    for N in refc.SPMM_WIDTHS:
+        r = reference_spmm(N, metrics.spmm_flops(m, N), A64, refc._spmm_operand(m, N))
+        out[f"N{N}"] = r if r is not None else {"unavailable": "the reference's generated SpMM is not present"}
+    return out
 
 
 def main():

@@ -13,8 +13,8 @@ Compiles the C restatement of the reference's generated executor
 and the MKL stand-in (mkl_standin/) used to run the reference's own
 generated C (tests/golden/make_golden.py, oracle/refc.py).  Where the
 reference tree is present (SABLE_REFERENCE_ROOT, else REFERENCE_ROOT), build()
-also runs the reference's own code generator for the timed CPU baseline
-(oracle/refc.py, into oracle/_ref/).
+also runs the reference's own code generators (SpMV and SpMM) for the timed
+CPU baselines (oracle/refc.py, into oracle/_ref/).
 """
 import os
 import pathlib
@@ -70,6 +70,7 @@ def build(force: bool = False, generate: bool = False) -> None:
     if generate and reference_root() is not None:
         from oracle import refc
         refc.generate(reference_root())
+        refc.generate_spmm(reference_root())
 
 
 if __name__ == "__main__":

@@ -23,3 +23,36 @@ def test_generated_sources_carry_only_the_listed_shims():
         assert len(re.findall(r"spmv_kernel(_2|_3)?\(y, x, val,", text)) > 1000
         assert "mkl_sparse_d_mv(SPARSE_OPERATION_NON_TRANSPOSE" in text
     assert "#pragma omp section" in (refc.OUT / "mt.c").read_text()
+
+
+def test_generated_spmm_sources_carry_only_the_listed_shims():
+    """The reference's SpMM program per width: the width macro, binary input
+    reads, the repeated timed region and the output format are the only
+    changes; every block of the matrix appears as one dense loop nest in the
+    thread functions, and the units together hold all thread functions."""
+    widths = [N for N in refc.SPMM_WIDTHS if refc.spmm_generated(N)]
+    if not widths:
+        pytest.skip("the reference's generated SpMM is not present on this host")
+    import json
+    from sable_gb300 import synth
+    m = synth.spmm_50k()
+    for N in widths:
+        d = refc._spmm_dir(N)
+        meta = json.loads((d / "meta.json").read_text())
+        assert meta["signature"] == refc._spmm_signature(m, N) and meta["density"] == 0
+        main = (d / "main.c").read_text()
+        assert main.startswith(f"#define SPMM_N {N}\n")
+        assert 'fopen("@VAL_PATH@", "rb")' in main and 'fopen("@X_PATH@", "rb")' in main
+        assert "fscanf" not in main and main.count("fread(") == 2
+        assert main.count("for (int sable_it = 0; sable_it < sable_bench; sable_it++) {") == 1
+        assert main.count("(unsigned long)((t2.tv_sec - t1.tv_sec) * 1e9 + (t2.tv_nsec - t1.tv_nsec))") == 1
+        assert 'printf("%.9g\\n", y[i*SPMM_N + j])' in main and 'printf("%f' not in main
+        funcs = sorted(u for u in meta["units"] if u != "main.c")
+        assert len(funcs) == refc.THREADS
+        nests = 0
+        for u in funcs:
+            body = (d / u).read_text()
+            assert body.startswith("extern float *x, *val, *y;\n")
+            assert f"void *{u[:-2]}();" in main and f"pthread_create(&tid[{u[4:-2]}], NULL, &{u[:-2]}, NULL);" in main
+            nests += len(re.findall(rf"for \(int k = 0; k < {N}; k\+\+\) \{{;y\[", body))
+        assert nests == len(m.bindx)
