@@ -12,7 +12,7 @@
 namespace {
 
 // Panel ring of a launch: stages of TERMS * hp * 32 bytes for the plan's
-// tallest tile, as many as fit (4..8) beside the X stages in the shared
+// tallest tile, as many as fit (4..12) beside the X stages in the shared
 // memory of one of three CTAs per SM.
 template <int NT, int TERMS>
 void umma_ring(int hp, int &bst, int &bstage) {

@@ -22,9 +22,9 @@
 //              blocks of hp x 32 bytes (hp = h rounded up to 16); one bulk
 //              copy (cp.async.bulk, mbarrier completion) brings TERMS of them
 //              into a ring of bst stages, bst - 2 steps ahead of the MMAs
-//              (the launch sizes the ring for 4..8 stages of its tallest
+//              (the launch sizes the ring for 4..12 stages of its tallest
 //              tile beside three CTAs per SM; an item with shorter tiles fits
-//              more of its own stages in the same bytes, up to 8).
+//              more of its own stages in the same bytes, up to 12).
 //   A operand  the 16 X rows of the step (NT floats each, from L2), loaded
 //              two steps ahead into registers with 16-byte loads (their row
 //              indices four steps ahead, so no load waits on another), split
@@ -48,7 +48,7 @@
 
 namespace {
 
-constexpr int UMMA_BST_MIN = 4, UMMA_BST_MAX = 8;   // panel-term stages (bulk-copy ring)
+constexpr int UMMA_BST_MIN = 4, UMMA_BST_MAX = 12;  // panel-term stages (bulk-copy ring)
 // X-term stages: the producers run up to NA - 1 steps ahead of the MMAs.
 // Two: a third stage takes the shared memory of two panel stages at three
 // CTAs per SM, and the shorter panel-copy lookahead lost more than the
@@ -60,6 +60,15 @@ constexpr int UMMA_THREADS = SABLE_THREADS + 32;   // producers + the issuer war
 // Dynamic shared memory of one CTA when three CTAs share an SM (228 KB less
 // the per-CTA reserve and static shared memory).
 constexpr int UMMA_SMEM_BUDGET = 75776;
+
+// A bounded mbarrier wait that first tests the phase without blocking, so
+// that a phase already complete costs no clock read.
+__device__ __forceinline__ bool umma_wait(unsigned bar, unsigned parity) {
+    unsigned done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+    return done != 0 || mbar_wait(bar, parity);
+}
 
 // Shared memory of a CTA: UMMA_NA stages of X terms, bst stages of panel
 // terms of bstage bytes, then the CSR row starts; the Y tile reuses the stage
@@ -78,19 +87,19 @@ struct UmmaSmem {
 };
 
 // Split four FP32 values into TERMS BF16 terms; t[k] packs the four k-th
-// terms (first value in the low half of t[k].x).
+// terms (first value in the low half of t[k].x).  One packed conversion per
+// pair of values (round to nearest, as the scalar conversion rounds).
 template <int TERMS>
 __device__ __forceinline__ void split4(const float4 v, uint2 (&t)[TERMS]) {
     float r0 = v.x, r1 = v.y, r2 = v.z, r3 = v.w;
 #pragma unroll
     for (int k = 0; k < TERMS; ++k) {
-        const __nv_bfloat16 b0 = __float2bfloat16_rn(r0), b1 = __float2bfloat16_rn(r1);
-        const __nv_bfloat16 b2 = __float2bfloat16_rn(r2), b3 = __float2bfloat16_rn(r3);
-        t[k] = make_uint2(pack2(b0, b1), pack2(b2, b3));
-        r0 -= __bfloat162float(b0);
-        r1 -= __bfloat162float(b1);
-        r2 -= __bfloat162float(b2);
-        r3 -= __bfloat162float(b3);
+        const __nv_bfloat162 p01 = __floats2bfloat162_rn(r0, r1), p23 = __floats2bfloat162_rn(r2, r3);
+        t[k] = make_uint2(*reinterpret_cast<const uint32_t *>(&p01), *reinterpret_cast<const uint32_t *>(&p23));
+        r0 -= __low2float(p01);
+        r1 -= __high2float(p01);
+        r2 -= __low2float(p23);
+        r3 -= __high2float(p23);
     }
 }
 
@@ -160,6 +169,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         const uint32_t idesc = umma_idesc_bf16(UMMA_M, hp, true);
         const int *colmap = reinterpret_cast<const int *>(R + c.xcol_off);
         const float *__restrict__ X = a.x;
+        const int64_t ldx = a.ldx;
         if (tid == 0) {
             for (int s = 0; s < bst; ++s) mbar_init(smem_addr(&s_full[s]));
             for (int s = 0; s < UMMA_NA; ++s) {
@@ -183,20 +193,29 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         // this thread's panel column within a step, and its X row at step j (-1: none)
         int k0, q0;
         umma_unit(tid, k0, q0);
+        const bool has_col = prod && tid < UNITS;
+        const int *colp = colmap + k0;
         auto col_row = [&](int j) -> int {
-            const int col = 16 * j + k0;
-            return (prod && tid < UNITS && j < nks && col < ncol) ? ld_pinned_s32(colmap + col) : -1;
+            return (has_col && 16 * j + k0 < ncol) ? ld_pinned_s32(colp + 16 * j) : -1;
         };
+        // this thread's X units, fixed for the item: the N-slice column of
+        // unit i (-1: past N or no unit) and the byte offset of its terms in
+        // an X stage (-1: no unit)
+        int ucol[UPT], uoff[UPT];
+#pragma unroll
+        for (int i = 0; i < UPT; ++i) {
+            const int u = tid + i * SABLE_THREADS;
+            int k, q;
+            umma_unit(u, k, q);
+            const bool has = prod && u < UNITS;
+            ucol[i] = has && n0 + 4 * q < a.N ? n0 + 4 * q : -1;
+            uoff[i] = has ? umma_mnmajor_off(4 * q, k) : -1;
+        }
         auto load_step = [&](int row, float4 (&dst)[UPT]) {
 #pragma unroll
             for (int i = 0; i < UPT; ++i) {
-                const int u = tid + i * SABLE_THREADS;
-                int k, q;
-                umma_unit(u, k, q);
-                const int n = n0 + 4 * q;
                 dst[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (prod && u < UNITS && row >= 0 && n < a.N)
-                    dst[i] = ld_pinned_f4(X + (int64_t)row * a.ldx + n);
+                if (row >= 0 && ucol[i] >= 0) dst[i] = ld_pinned_f4(X + (int64_t)row * ldx + ucol[i]);
             }
         };
         // The producer warps and the issuer run decoupled and hand the stages
@@ -223,7 +242,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
             // ks + 4.  false: stop (warp-uniform).
             auto pstep = [&](int ks, float4 (&slot)[UPT], int &cm) -> bool {
                 if (ks >= UMMA_NA) {   // the products of step ks - NA have read this X stage
-                    const bool ok = mbar_wait(smem_addr(&s_done[ks % UMMA_NA]), (uint32_t)(((ks - UMMA_NA) / UMMA_NA) & 1));
+                    const bool ok = umma_wait(smem_addr(&s_done[ks % UMMA_NA]), (uint32_t)(((ks - UMMA_NA) / UMMA_NA) & 1));
                     const bool stop = *reinterpret_cast<volatile int *>(&s_stop) != 0;
                     if (__any_sync(FULL, !ok || stop)) {
                         if (!ok) s_stop = 1;
@@ -238,15 +257,11 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 unsigned char *As = smem + L::OFF_A + (ks % UMMA_NA) * L::A_STAGE;
 #pragma unroll
                 for (int i = 0; i < UPT; ++i) {
-                    const int u = tid + i * SABLE_THREADS;
-                    if (u < UNITS) {
-                        int k, q;
-                        umma_unit(u, k, q);
+                    if (uoff[i] >= 0) {
                         uint2 t[TERMS];
                         split4<TERMS>(cur[i], t);
-                        const int off = umma_mnmajor_off(4 * q, k);
 #pragma unroll
-                        for (int e = 0; e < TERMS; ++e) *reinterpret_cast<uint2 *>(As + e * (UMMA_M * 32) + off) = t[e];
+                        for (int e = 0; e < TERMS; ++e) *reinterpret_cast<uint2 *>(As + e * (UMMA_M * 32) + uoff[i]) = t[e];
                     }
                 }
                 fence_async_smem();
@@ -260,49 +275,65 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
             }
         } else if (issuer) {
             int issued = look < nks ? look : nks, landed = 0, committed = 0;
+            // ring positions as counters, so that the loop divides by no
+            // runtime ring depth: panel stage s of step ks with its phase
+            // parity sph, and stage sj of step ks + look, which the step's
+            // copy fills from src
+            int s = 0, sj = look;
+            uint32_t sph = 0;
+            const unsigned char *src = planes + (size_t)look * step_src;
+            // descriptors of the stage bases: a stage or term offset adds its
+            // count of 16-byte units to the start-address field (shared
+            // addresses stay below 256 KB, so the 14-bit field never carries)
+            const uint64_t ad0 = umma_sdesc(a_base, UMMA_MN_LBO, UMMA_MN_SBO);
+            const uint64_t bd0 = umma_sdesc(b_base, UMMA_KM_LBO, UMMA_KM_SBO);
+            const uint32_t bterm16 = (uint32_t)hp * 2u, bstage16 = (uint32_t)bstage >> 4;
             for (int ks = 0; ks < nks; ++ks) {
                 if (*reinterpret_cast<volatile int *>(&s_stop)) break;
                 // the products of step ks - 2 have read the panel stage that
-                // step ks + look takes
-                if (ks >= 2 && !mbar_wait(smem_addr(&s_done[(ks - 2) % UMMA_NA]), (uint32_t)(((ks - 2) / UMMA_NA) & 1))) {
+                // step ks + look takes (waited for only where that step exists)
+                if (ks >= 2 && ks + look < nks && !umma_wait(smem_addr(&s_done[(ks - 2) % UMMA_NA]), (uint32_t)(((ks - 2) / UMMA_NA) & 1))) {
                     s_stop = 1;
                     break;
                 }
-                const int j = ks + look;
-                if (j < nks) {
-                    tma_record(smem_addr(&s_full[j % bst]), smem + L::OFF_B + (j % bst) * bstage,
-                               planes + (size_t)j * step_src, copy_bytes);
-                    issued = j + 1;
+                if (ks + look < nks) {
+                    tma_record(smem_addr(&s_full[sj]), smem + L::OFF_B + sj * bstage, src, copy_bytes);
+                    issued = ks + look + 1;
                 }
-                const int s = ks % bst;
-                if (!mbar_wait(smem_addr(&s_afull[ks % UMMA_NA]), (uint32_t)((ks / UMMA_NA) & 1))) {
+                src += step_src;
+                sj = sj + 1 == bst ? 0 : sj + 1;
+                if (!umma_wait(smem_addr(&s_afull[ks % UMMA_NA]), (uint32_t)((ks / UMMA_NA) & 1))) {
                     s_stop = 1;
                     break;
                 }
-                if (!mbar_wait(smem_addr(&s_full[s]), (uint32_t)((ks / bst) & 1))) {
+                if (!umma_wait(smem_addr(&s_full[s]), sph)) {
                     s_stop = 1;
                     break;
                 }
                 landed = ks + 1;
                 tc_fence_after();
-                const uint32_t a_st = a_base + (uint32_t)((ks % UMMA_NA) * L::A_STAGE);
-                const uint32_t b_st = b_base + (uint32_t)(s * bstage);
+                const uint64_t ad_st = ad0 + (uint64_t)((ks % UMMA_NA) * (L::A_STAGE >> 4));
+                const uint64_t bd_st = bd0 + (uint64_t)((uint32_t)s * bstage16);
                 // products (x term, panel term), smallest first
                 constexpr int PA[6] = {1, 0, 2, 0, 1, 0}, PB[6] = {1, 2, 0, 1, 0, 0};
                 constexpr int QA[3] = {0, 1, 0}, QB[3] = {1, 0, 0};
 #pragma unroll
                 for (int p = 0; p < NPROD; ++p) {
                     const int ta = TERMS == 3 ? PA[p] : QA[p], tb = TERMS == 3 ? PB[p] : QB[p];
-                    const uint64_t ad = umma_sdesc(a_st + (uint32_t)(ta * UMMA_M * 32), UMMA_MN_LBO, UMMA_MN_SBO);
-                    const uint64_t bd = umma_sdesc(b_st + (uint32_t)(tb * hp * 32), UMMA_KM_LBO, UMMA_KM_SBO);
+                    const uint64_t ad = ad_st + (uint64_t)(ta * (UMMA_M * 32 / 16));
+                    const uint64_t bd = bd_st + (uint64_t)((uint32_t)tb * bterm16);
                     umma_bf16(taddr, ad, bd, idesc, (ks > 0 || p > 0) ? 1u : 0u);
                 }
                 umma_commit(smem_addr(&s_done[ks % UMMA_NA]));
                 committed = ks + 1;
+                if (++s == bst) {
+                    s = 0;
+                    sph ^= 1u;
+                }
             }
             // every panel copy issued has landed before the CTA exits
             for (int j = landed; j < issued; ++j)
-                if (!mbar_wait(smem_addr(&s_full[j % bst]), (uint32_t)((j / bst) & 1))) s_stop = 1;
+                if (!umma_wait(smem_addr(&s_full[j % bst]), (uint32_t)((j / bst) & 1))) s_stop = 1;
             s_committed = committed;
         }
         __syncthreads();
@@ -313,7 +344,7 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         // commit covers them all.
         if (committed > 0) {
             const int last = committed - 1;
-            if (!mbar_wait(smem_addr(&s_done[last % UMMA_NA]), (uint32_t)((last / UMMA_NA) & 1))) s_stop = 1;
+            if (!umma_wait(smem_addr(&s_done[last % UMMA_NA]), (uint32_t)((last / UMMA_NA) & 1))) s_stop = 1;
         }
         tc_fence_before();
         __syncthreads();
