@@ -170,26 +170,6 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         const int *colmap = reinterpret_cast<const int *>(R + c.xcol_off);
         const float *__restrict__ X = a.x;
         const int64_t ldx = a.ldx;
-        if (tid == 0) {
-            for (int s = 0; s < bst; ++s) mbar_init(smem_addr(&s_full[s]));
-            for (int s = 0; s < UMMA_NA; ++s) {
-                mbar_init(smem_addr(&s_done[s]));
-                mbar_init_count(smem_addr(&s_afull[s]), SABLE_THREADS / 32);
-            }
-            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-            s_stop = 0;
-            s_committed = 0;
-        }
-        if (warp == 0) tmem_alloc(smem_addr(&s_taddr), ncols);
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        const uint32_t taddr = s_taddr;
-        // panel copies of the first `look` steps
-        if (issuer)
-            for (int j = 0; j < look && j < nks; ++j)
-                tma_record(smem_addr(&s_full[j]), smem + L::OFF_B + j * bstage, planes + (size_t)j * step_src,
-                           copy_bytes);
         // this thread's panel column within a step, and its X row at step j (-1: none)
         int k0, q0;
         umma_unit(tid, k0, q0);
@@ -218,6 +198,35 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 if (row >= 0 && ucol[i] >= 0) dst[i] = ld_pinned_f4(X + (int64_t)row * ldx + ucol[i]);
             }
         };
+        // The issuer initialises the barriers and starts the first panel
+        // copies, and the producers load the X rows of the first two steps,
+        // before the CTA barrier that publishes the barriers and the TMEM
+        // address, so that those latencies overlap the TMEM allocation.
+        float4 xr0[UPT], xr1[UPT];   // X values of the next even / odd step
+        int cm0 = -1, cm1 = -1;
+        if (issuer) {
+            for (int s = 0; s < bst; ++s) mbar_init(smem_addr(&s_full[s]));
+            for (int s = 0; s < UMMA_NA; ++s) {
+                mbar_init(smem_addr(&s_done[s]));
+                mbar_init_count(smem_addr(&s_afull[s]), SABLE_THREADS / 32);
+            }
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            s_stop = 0;
+            s_committed = 0;
+            for (int j = 0; j < look && j < nks; ++j)   // panel copies of the first `look` steps
+                tma_record(smem_addr(&s_full[j]), smem + L::OFF_B + j * bstage, planes + (size_t)j * step_src,
+                           copy_bytes);
+        } else if (prod) {
+            load_step(col_row(0), xr0);
+            load_step(col_row(1), xr1);
+            cm0 = col_row(2);
+            cm1 = col_row(3);
+        }
+        if (warp == 0) tmem_alloc(smem_addr(&s_taddr), ncols);
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        const uint32_t taddr = s_taddr;
         // The producer warps and the issuer run decoupled and hand the stages
         // over through mbarriers: a producer warp writes its part of the X
         // terms of step ks into stage ks % NA, fences them to the async proxy
@@ -232,10 +241,6 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         // out sets s_stop, which both loops check, so an error ends the item
         // after at most one more bounded wait per thread.
         if (prod) {
-            float4 xr0[UPT], xr1[UPT];   // X values of the next even / odd step
-            load_step(col_row(0), xr0);
-            load_step(col_row(1), xr1);
-            int cm0 = col_row(2), cm1 = col_row(3);
             // Step ks: its X values are in `slot` (loaded two steps earlier),
             // which then receives those of step ks + 2, whose row `cm` was read
             // two steps earlier still; `cm` then receives the row of step
