@@ -33,8 +33,9 @@ reference's own generated SpMM (gen_multi_threaded_spmm, density 0 as its
 benchmark, FP32, pthreads) at N = 32 and 128, compiled in the same pool.
 The GPU arm's cpu_baseline reports the same SpMV program when it is already
 compiled on the host, else the port, for the same number of iterations; its
-SpMM cpu_baselines run the reference's generated SpMM (compiled on first use
-where the reference arm has not compiled it, about a minute).  Under torchrun each rank runs its own seeded
+SpMM cpu_baselines run the reference's generated SpMM (the median of four
+runs; compiled at start-up, before any GPU work, where the reference arm has
+not compiled it, about a minute).  Under torchrun each rank runs its own seeded
 replica (weak scaling, no collective on the data path); with --strong the
 ranks instead take block-row shards of the one matrix, balanced by algorithmic
 bytes (sable_gb300.shard), each writing its own rows of y (strong scaling).
@@ -270,12 +271,23 @@ def sampled_error(A64, Y, Xh, rows: int = 4000) -> np.ndarray:
     return np.abs(np.asarray(Y, np.float64)[sel] - ref) / np.maximum(scale, 1e-300)
 
 
+def compile_reference_spmm() -> None:
+    """Compile the reference's generated SpMM programs that are present and
+    not yet compiled on this host (both widths in one pool, about a minute),
+    so that no compilation runs right before a timed CPU baseline (a run
+    straight after the compilation measured up to 4x slower)."""
+    from oracle import refc
+    widths = [w for w in refc.SPMM_WIDTHS if refc.spmm_generated(w) and not refc.spmm_compiled(w)]
+    if widths:
+        refc.compile((), spmm_widths=widths)
+
+
 def reference_spmm(N: int, F: float, A64, Xh, runs: int = 4):
     """The reference's own generated multi-threaded SpMM at width N
     (oracle/refc.py: gen_multi_threaded_spmm with density 0, as its own
-    benchmark runs it; FP32, its CFLAGS for this host; both widths compiled
-    on first use, about a minute), or None where its sources were not
-    generated.  `runs` timed runs after one dropped cold run."""
+    benchmark runs it; FP32, its CFLAGS for this host; compiled first where
+    needed), or None where its sources were not generated.  The median of
+    `runs` timed runs after one dropped cold run."""
     from oracle import refc
     if not refc.spmm_generated(N):
         return None
@@ -283,11 +295,11 @@ def reference_spmm(N: int, F: float, A64, Xh, runs: int = 4):
         refc.compile((), spmm_widths=[w for w in refc.SPMM_WIDTHS if refc.spmm_generated(w)])
     r = refc.run_spmm(N, runs + 1)
     t = np.asarray(r["times_ns"][1:], np.float64) * 1e-9
-    ms = float(np.mean(t)) * 1e3
+    ms = float(np.median(t)) * 1e3
     rel = sampled_error(A64, r["Y"], Xh)
     return {"value": round(F / (ms * 1e-3) / 1e9, 1), "unit": "GFLOP/s", "ms": round(ms, 3),
             "cores": int(r["threads"]), "kind": "reference",
-            "sample": f"full matrix, width {N}, {len(t)} timed runs after one dropped cold run of the reference's "
+            "sample": f"full matrix, width {N}, median of {len(t)} timed runs after one dropped cold run of the reference's "
                       f"own generated multi-threaded SpMM (gen_multi_threaded_spmm, density 0 as its benchmark, "
                       f"{r['threads']} pthreads, FP32, its CFLAGS); max error vs FP64 {float(rel.max()):.1e} of "
                       f"|A||X| over 4000 sampled rows"}
@@ -473,6 +485,8 @@ def run_sable(args):
     import torch
     from sable_gb300 import _lib, autotune, blockmodel, convert
     from sable_gb300.plan import Plan
+    if int(os.environ.get("RANK", "0")) == 0 and not args.quick and not args.no_cpu_baseline:
+        compile_reference_spmm()   # before any GPU work, not beside it
     world, rank, local = dist_setup()
     torch.cuda.set_device(local)
     if args.strong and world > 1:
