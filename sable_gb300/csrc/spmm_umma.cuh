@@ -34,12 +34,16 @@
 //              proxy and arrives on the stage's "X ready" mbarrier.
 //   MMA        the issuer waits for the stage's "X ready" barrier and the
 //              step's panel copy, issues the products (tcgen05.mma.cta_group::1
-//              .kind::f16, M = 128, N = hp, K = 16) and commits them to the
-//              stage's "done" mbarrier; the producers wait on it before they
-//              reuse the X stage, the issuer two steps later before it reuses
-//              the panel stage.  No CTA-wide barrier inside the K loop.
+//              .kind::f16, M = 128, N = hp, K = 16; for split3 tiles of at
+//              most 64 rows four MMAs, two of them with N = 2 hp over two
+//              panel terms at once into two accumulator ranges) and commits
+//              them to the stage's "done" mbarrier; the producers wait on it
+//              before they reuse the X stage, the issuer two steps later
+//              before it reuses the panel stage.  No CTA-wide barrier inside
+//              the K loop.
 // After the last step the accumulator is read with tcgen05.ld into the Y
-// tile in shared memory (lane m, column n -> Y[n][m]); TMEM is freed on every
+// tile in shared memory (lane m, column n -> Y[n][m]; with two ranges, their
+// sum); TMEM is freed on every
 // path.  Every wait is bounded (WAIT_NS); on expiry the error flag is set, the
 // CTA stops issuing work, waits (bounded) for what it issued and frees TMEM.
 #pragma once
@@ -162,11 +166,17 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
         const int bstage = TERMS * hp * 32;
         const int bst = min(UMMA_BST_MAX, (ring_bst * ring_bstage) / bstage);
         const int look = bst - 2;    // panel copies run this many steps ahead
-        const uint32_t ncols = umma_tmem_cols(hp);
+        // split3 tiles of at most 64 rows issue their six products as four
+        // MMAs: two take the first two panel terms at once (N = 2 hp: the
+        // term blocks lie one after another, which is the K-major layout of
+        // one operand of 2 hp rows) into two accumulator ranges that the
+        // epilogue adds
+        const bool stacked = TERMS == 3 && hp <= 64;
+        const uint32_t ncols = umma_tmem_cols(stacked ? 2 * hp : hp);
         const uint32_t step_src = 3u * (uint32_t)hp * 32u;           // bytes of a step in `planes`
         const uint32_t copy_bytes = (uint32_t)TERMS * (uint32_t)hp * 32u;
         const uint32_t a_base = smem_addr(smem + L::OFF_A), b_base = smem_addr(smem + L::OFF_B);
-        const uint32_t idesc = umma_idesc_bf16(UMMA_M, hp, true);
+        const uint32_t idesc = umma_idesc_bf16(UMMA_M, hp, true), idesc2 = umma_idesc_bf16(UMMA_M, 2 * hp, true);
         const int *colmap = reinterpret_cast<const int *>(R + c.xcol_off);
         const float *__restrict__ X = a.x;
         const int64_t ldx = a.ldx;
@@ -322,12 +332,22 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 // products (x term, panel term), smallest first
                 constexpr int PA[6] = {1, 0, 2, 0, 1, 0}, PB[6] = {1, 2, 0, 1, 0, 0};
                 constexpr int QA[3] = {0, 1, 0}, QB[3] = {1, 0, 0};
+                if (stacked) {
+                    // x1 [b0 b1] (at step 0 it initialises both ranges), x0 b2
+                    // into the first range, x2 b0 into the second, x0 [b0 b1]
+                    constexpr uint64_t AT = UMMA_M * 32 / 16;   // one X term block, 16-byte units
+                    umma_bf16(taddr, ad_st + AT, bd_st, idesc2, ks > 0 ? 1u : 0u);
+                    umma_bf16(taddr, ad_st, bd_st + (uint64_t)(2u * bterm16), idesc, 1u);
+                    umma_bf16(taddr + (uint32_t)hp, ad_st + 2 * AT, bd_st, idesc, 1u);
+                    umma_bf16(taddr, ad_st, bd_st, idesc2, 1u);
+                } else {
 #pragma unroll
-                for (int p = 0; p < NPROD; ++p) {
-                    const int ta = TERMS == 3 ? PA[p] : QA[p], tb = TERMS == 3 ? PB[p] : QB[p];
-                    const uint64_t ad = ad_st + (uint64_t)(ta * (UMMA_M * 32 / 16));
-                    const uint64_t bd = bd_st + (uint64_t)((uint32_t)tb * bterm16);
-                    umma_bf16(taddr, ad, bd, idesc, (ks > 0 || p > 0) ? 1u : 0u);
+                    for (int p = 0; p < NPROD; ++p) {
+                        const int ta = TERMS == 3 ? PA[p] : QA[p], tb = TERMS == 3 ? PB[p] : QB[p];
+                        const uint64_t ad = ad_st + (uint64_t)(ta * (UMMA_M * 32 / 16));
+                        const uint64_t bd = bd_st + (uint64_t)((uint32_t)tb * bterm16);
+                        umma_bf16(taddr, ad, bd, idesc, (ks > 0 || p > 0) ? 1u : 0u);
+                    }
                 }
                 umma_commit(smem_addr(&s_done[ks % UMMA_NA]));
                 committed = ks + 1;
@@ -364,6 +384,12 @@ __device__ __forceinline__ void spmm_umma_item(const unsigned char *R, const Mat
                 for (int c0 = 16 * (warp >> 2); c0 < hp; c0 += 32) {
                     uint32_t r[16];
                     tmem_ld16(taddr + ((uint32_t)(32 * quad) << 16) + (uint32_t)c0, r);
+                    if (stacked) {   // plus the second accumulator range
+                        uint32_t r2[16];
+                        tmem_ld16(taddr + ((uint32_t)(32 * quad) << 16) + (uint32_t)(hp + c0), r2);
+#pragma unroll
+                        for (int jj = 0; jj < 16; ++jj) r[jj] = __float_as_uint(__uint_as_float(r[jj]) + __uint_as_float(r2[jj]));
+                    }
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj)
                         if (c0 + jj < h) ys[(c0 + jj) * NT + m] = __uint_as_float(r[jj]);
