@@ -56,3 +56,49 @@ def test_generated_spmm_sources_carry_only_the_listed_shims():
             assert f"void *{u[:-2]}();" in main and f"pthread_create(&tid[{u[4:-2]}], NULL, &{u[:-2]}, NULL);" in main
             nests += len(re.findall(rf"for \(int k = 0; k < {N}; k\+\+\) \{{;y\[", body))
         assert nests == len(m.bindx)
+
+
+def test_spmm_program_pipeline_on_a_small_matrix(tmp_path):
+    """The SpMM harness end to end on a 400 x 400 matrix (where the reference
+    tree is present): the reference's generator with the width as SPMM_N, the
+    listed substitutions, the cut into one unit per thread function, binary
+    inputs, three timed runs; Y of the last run against the FP64 oracle."""
+    import subprocess
+
+    import numpy as np
+
+    from oracle import build as ob
+    from oracle import oracle
+    from sable_gb300 import synth
+    root = ob.reference_root()
+    if root is None:
+        pytest.skip("the reference tree is not present on this host")
+    ob.build()
+    m = synth.spmm_50k(seed=1010, n=400, parts=10, p=0.3)
+    N = 8
+    a = m.arrays()
+    args = [list(map(float, a[0]))] + [list(map(int, v)) for v in a[1:]]
+    gen = tmp_path / "gen"
+    gen.mkdir()
+    refc._spmm_codegen(root, N).gen_multi_threaded_spmm(4, *args, 0, str(gen), "spmm", str(gen))
+    units = refc._spmm_split(refc._spmm_shim((gen / "spmm.c").read_text(), N, len(args[0])))
+    assert sorted(units) == ["func0.c", "func1.c", "func2.c", "func3.c", "main.c"]
+    valf, xf = tmp_path / "val.f32", tmp_path / "x.f32"
+    np.asarray(m.val, np.float32).tofile(valf)
+    X = synth.dense_operand(m.n_cols, N, 3)
+    X.tofile(xf)
+    objs = []
+    for name, body in units.items():
+        src = tmp_path / name
+        src.write_text(body.replace("@VAL_PATH@", str(valf)).replace("@X_PATH@", str(xf)))
+        objs.append(str(tmp_path / (name[:-2] + ".o")))
+        subprocess.run(["gcc", "-O1", "-c", str(src), "-o", objs[-1]], check=True, capture_output=True)
+    exe = tmp_path / "spmm"
+    subprocess.run(["gcc", "-o", str(exe), *objs, "-lpthread"], check=True, capture_output=True)
+    r = subprocess.run([str(exe)], env={"SABLE_BENCH": "3"}, capture_output=True, text=True, check=True)
+    lines = r.stdout.split("\n", 3)
+    assert all(re.fullmatch(r"spmm = \d+", ln) for ln in lines[:3]), lines[:3]
+    Y = np.array(lines[3].split(), dtype=np.float64).reshape(m.n_rows, N)
+    Yr, Ya = oracle.spmm_vbr(m, X.astype(np.float64))
+    rep = oracle.report(Y, Yr, Ya, 1e-5)
+    assert rep["pass"], rep
